@@ -1,0 +1,392 @@
+"""Benchmark: FP32 TSQR of a 4,194,304 x 32 matrix on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--m M] [--n N] [--form auto|plain|tf32x3|bf16x3]
+
+One step = one TSQR (A <- Q, R) of the whole matrix through libtsqr_gb300's C
+ABI.  Input: A = U diag(sigma) V^T with U, V orthonormal (QR of seeded
+Gaussians) and sigma geometric from 1 to 1e-6, generated on the device
+(synthetic, seeded).  Before every step A is restored from a pristine copy
+and L2 is flushed by writing a 256 MiB buffer; both happen outside the
+per-step CUDA-event pair, so `value` is the device time of the factorisation
+alone, with the input resident in HBM.  A (512 MiB) is itself larger than L2.
+
+Printed (rank 0, one JSON line):
+  value        algorithmic TFLOP/s, F = 4 m n^2 - 4/3 n^3 (geqrf + orgqr)
+  roofline     the dominant kernel's achieved HBM GB/s (algorithmic bytes per
+               launch / its CUDA-event time) against the measured HBM peak
+  step_roofline the whole step against max(F / FP32 peak, bytes / HBM peak)
+  e2e          the same metric through the C ABI with host buffers: pinned
+               H2D of A, the factorisation, D2H of Q and R, every step
+  cpu_baseline the oracle's restatement of the reference TSQR (FP32, OpenMP)
+               on the host cores, on the same workload
+  forms        each precision form's time and FP64-checked errors
+
+--impl reference: the reference has no CPU path and its own code is CUDA, so
+this arm times the oracle's restatement of the reference algorithm
+(TallShinnyQR.h:86-148 schedule, kernelQR.h:69-291 tile QR, FP32) on all host
+cores of rank 0, on the same workload; other ranks exit without work.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "QR TFLOP/s & % roofline, tensor-core vs plain FP32 at equal FP64-oracle error"
+
+
+def flops(m, n):
+    return 4.0 * m * n * n - 4.0 / 3.0 * n ** 3
+
+
+def alg_bytes(m, n, es=4):
+    return (2.0 * m * n + n * n) * es
+
+
+def peaks():
+    p = {"hbm_gbs": 6800.0, "source": "fallback"}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        p["hbm_gbs"] = float(d["hbm_gbs"])
+        p["sm_max_mhz"] = float(d.get("sm_max_mhz", 2070.0))
+        p["source"] = "measured"
+    except Exception:
+        p["sm_max_mhz"] = 2070.0
+    # FP32 CUDA-core peak: SMs x 128 FMA lanes x 2 flop x max SM clock
+    # (nominal; not in the measured file).
+    p["fp32_tflops"] = None
+    return p
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_input(m, n, seed, device):
+    """A = U diag(sigma) V^T, sigma geometric 1 -> 1e-6 (condition 1e6)."""
+    import torch
+    g = torch.Generator(device=device).manual_seed(seed)
+    G = torch.randn((m, n), generator=g, device=device, dtype=torch.float64)
+    U, _ = torch.linalg.qr(G)
+    H = torch.randn((n, n), generator=g, device=device, dtype=torch.float64)
+    V, _ = torch.linalg.qr(H)
+    sig = torch.logspace(0, -6, n, device=device, dtype=torch.float64)
+    A = (U * sig) @ V.t()
+    del G, U
+    return A.float().t().contiguous().t()  # column-major m x n
+
+
+def check_errors(A0, Q, R):
+    """FP64 backward error and orthogonality on the device (checker)."""
+    import torch
+    A64 = A0.double()
+    E = A64 - Q.double() @ R.double()
+    back = (torch.linalg.norm(E) / torch.linalg.norm(A64)).item()
+    Qd = Q.double()
+    G = Qd.t() @ Qd
+    orth = torch.linalg.norm(G - torch.eye(G.shape[0], dtype=G.dtype, device=G.device)).item()
+    return back, orth
+
+
+def run_form(tg, A0, form, steps, warmup, device, flush):
+    import torch
+    m, n = A0.shape
+    A = tg.empty_colmajor(m, n, torch.float32, device)
+    R = tg.empty_colmajor(n, n, torch.float32, device)
+    nb = tg.workspace_bytes(m, n, torch.float32, precision=form)
+    work = torch.empty(max(nb, 1), dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream()
+
+    def one(timed_events=None):
+        A.copy_(A0)
+        flush.zero_()
+        if timed_events is not None:
+            timed_events[0].record(stream)
+        tg.tsqr_(A, R, precision=form, work=work, stream=stream)
+        if timed_events is not None:
+            timed_events[1].record(stream)
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        one(evs[k])
+    torch.cuda.synchronize()
+    times = [a.elapsed_time(b) for a, b in evs]
+    back, orth = check_errors(A0, A, R)
+    # per-launch device times of one more step, same stream, same buffers
+    A.copy_(A0)
+    flush.zero_()
+    launches = tg.profile_("tsqr", A, R, precision=form, work=work, stream=stream)
+    return {"ms": sum(times) / len(times), "ms_min": min(times), "backward": back, "orth": orth,
+            "launches": launches}
+
+
+def run_e2e(tg, A0, form, steps, warmup, device):
+    """Host buffers: pinned H2D of A, factorisation, D2H of Q and R."""
+    import torch
+    m, n = A0.shape
+    hA = torch.empty((n, m), dtype=torch.float32, pin_memory=True)
+    hA.copy_(A0.t())
+    hQ = torch.empty((n, m), dtype=torch.float32, pin_memory=True)
+    hR = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
+    A = tg.empty_colmajor(m, n, torch.float32, device)
+    R = tg.empty_colmajor(n, n, torch.float32, device)
+    nb = tg.workspace_bytes(m, n, torch.float32, precision=form)
+    work = torch.empty(max(nb, 1), dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream()
+
+    def one():
+        A.t().copy_(hA, non_blocking=True)
+        tg.tsqr_(A, R, precision=form, work=work, stream=stream)
+        hQ.copy_(A.t(), non_blocking=True)
+        hR.copy_(R.t(), non_blocking=True)
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for _ in range(steps):
+        one()
+    e.record(stream)
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / steps
+    return {"ms": ms, "h2d": m * n * 4, "d2h": m * n * 4 + n * n * 4}
+
+
+def cpu_port(m, n, budget_s=20.0, seed=0):
+    """The oracle's restatement of the reference TSQR (FP32) on the host."""
+    import numpy as np
+    from oracle import oracle as orc
+    cores = len(os.sched_getaffinity(0))
+    orc.set_num_threads(cores)
+    A = orc.fill_uniform(m, n, np.float32, seed=seed)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        orc.ref_tsqr(A)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or reps >= 3:
+            break
+    sec = el / reps
+    return {"value": flops(m, n) / sec / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+            "sample": "full %dx%d FP32 TSQR, %d repetition(s), %.3f s each" % (m, n, reps, sec)}
+
+
+def cpu_lapack(m, n, seed=0):
+    """LAPACK sgeqrf + sorgqr (scipy's OpenBLAS) on the host, for context."""
+    try:
+        import numpy as np
+        import scipy.linalg.lapack as la
+    except Exception as e:  # pragma: no cover
+        return {"unavailable": str(e)}
+    rng = np.random.default_rng(seed)
+    A = np.asfortranarray(rng.uniform(-1, 1, (m, n)).astype(np.float32))
+    t0 = time.perf_counter()
+    qr, tau, work, info = la.sgeqrf(A)
+    q, work, info = la.sorgqr(qr, tau)
+    sec = time.perf_counter() - t0
+    return {"value": flops(m, n) / sec / 1e12, "unit": "TFLOP/s", "cores": len(os.sched_getaffinity(0)),
+            "kind": "lapack sgeqrf+sorgqr (OpenBLAS via scipy)", "seconds": sec}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--m", type=int, default=4194304)
+    ap.add_argument("--n", type=int, default=32)
+    ap.add_argument("--form", default="auto")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local = dist_env()
+    m, n = args.m, args.n
+    F = flops(m, n)
+    workload = "TSQR FP32 m=%d n=%d, A overwritten by the explicit thin Q, R written" % (m, n)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        t = cpu_port(m, n, budget_s=1e9)  # each step a full factorisation
+        times = []
+        import numpy as np
+        from oracle import oracle as orc
+        A = orc.fill_uniform(m, n, np.float32)
+        for _ in range(min(args.warmup, 1)):
+            orc.ref_tsqr(A)
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            orc.ref_tsqr(A)
+            times.append(time.perf_counter() - t0)
+        sec = sum(times) / len(times)
+        val = F / sec / 1e12
+        out = {"metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic: reference input stream (uniform[-1,1), "
+               "std::default_random_engine(0))", "impl": "reference",
+               "config": {"workload": workload, "parallelism": "host cores, OpenMP over row chunks"},
+               "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": t["cores"], "kind": "port",
+                                "sample": "full %dx%d FP32 TSQR per step" % (m, n)},
+               "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return 0
+
+    import torch
+    import tsqr_gb300 as tg
+
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    tg.lib()
+    pk = peaks()
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    fp32_peak = sms * 128 * 2 * pk["sm_max_mhz"] * 1e6 / 1e12
+
+    A0 = make_input(m, n, 1234 + rank, device)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    forms = ["plain", "tf32x3"] if args.form == "auto" else [args.form]
+    results = {}
+    sampler = ClockSampler(local)
+    for f in forms:
+        try:
+            if ws > 1:
+                dist.barrier()
+            torch.cuda.synchronize()
+            if f == forms[0]:
+                sampler.start()
+            results[f] = run_form(tg, A0, f, args.steps, args.warmup, device, flush)
+        except tg.TsqrError as e:
+            results[f] = {"unsupported": str(e)}
+    clocks = sampler.stop()
+    u = 2.0 ** -24
+    ok = {f: r for f, r in results.items() if "ms" in r and r["backward"] <= 1e-5 and r["orth"] <= 1e-5}
+    head = min(ok, key=lambda f: ok[f]["ms"]) if ok else forms[0]
+    r = results[head]
+    ms = r["ms"]
+    if ws > 1:
+        t = torch.tensor([ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+    value = ws * F / (ms * 1e-3) / 1e12
+
+    # dominant kernel: the launch with the largest device time
+    la = r["launches"]
+    dom_tag, dom_ms = max(la, key=lambda x: x[1])
+    kind = dom_tag // 1000
+    level = dom_tag % 1000
+    # algorithmic bytes of a level-0 launch: the tile data read + written once
+    # (factor: A in, V out; apply: V in, Q out) plus the n x n per tile R/B.
+    dom_bytes = 2.0 * m * n * 4 if level == 0 else None
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9 if dom_bytes else None
+    roof_t = max(F / (fp32_peak * 1e12), alg_bytes(m, n) / (pk["hbm_gbs"] * 1e9))
+    e2e = run_e2e(tg, A0, head, max(3, args.steps // 4), 2, device)
+    e2e_val = ws * F / (e2e["ms"] * 1e-3) / 1e12
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_port(m, n)
+        lap = cpu_lapack(m, n)
+    else:
+        lap = None
+    nl = len(la)
+    out = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: A = U diag(sigma) V^T, U,V from QR of seeded Gaussians, sigma geometric 1..1e-6",
+        "config": {"workload": workload, "form": head, "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "flushed (256 MiB write) before every step; A (%d MiB) > L2" % (m * n * 4 >> 20),
+                   "input_restore": "A restored from a pristine copy before every step, outside the timed pair"},
+        "errors": {"backward": r["backward"], "orth": r["orth"], "bar": 1e-5},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": None,
+                     "kernel": ("factor" if kind == 1 else "apply" if kind == 2 else "tc") + "_level%d" % level,
+                     "kernel_ms": dom_ms, "peak_source": pk["source"]},
+        "step_roofline": {"time_ms": roof_t * 1e3, "frac": roof_t * 1e3 / ms, "fp32_peak_tflops": fp32_peak,
+                          "fp32_peak_source": "nominal: SMs x 128 lanes x 2 x max SM clock",
+                          "hbm_gbs": pk["hbm_gbs"], "flops": F, "bytes": alg_bytes(m, n)},
+        "e2e": {"value": e2e_val, "unit": "TFLOP/s", "h2d_bytes_per_step": e2e["h2d"],
+                "d2h_bytes_per_step": e2e["d2h"], "ms_per_step": e2e["ms"]},
+        "cpu_baseline": cpu, "cpu_lapack": lap,
+        "clocks": clocks, "gpu_launches": nl * args.steps, "launches_per_step": nl,
+        "forms": {f: ({"ms": v["ms"], "tflops": F / (v["ms"] * 1e-3) / 1e12, "backward": v["backward"],
+                       "orth": v["orth"]} if "ms" in v else v) for f, v in results.items()},
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,115 @@
+/*
+ * tsqr_gb300.h -- C ABI of the GB300 tall-skinny QR library.
+ *
+ * Every entry point takes plain device pointers, sizes and a stream handle
+ * (a cudaStream_t passed as void*; NULL = the legacy default stream, where
+ * the reference launches).  Matrices are column-major, as in the reference
+ * (lda >= m, A[i + j*lda]).  On success A is overwritten by the thin Q
+ * (m x n) and R (n x n, ldr) is fully written, zeros below the diagonal
+ * included.  Calls are asynchronous on `stream`; they never assert, never
+ * print and never exit: every failure comes back as a tsqr_status.
+ *
+ * Reference interfaces these replace (dajunHuang/tsqr):
+ *   template<T> void tsqr(int m,int n,T*A,int lda,T*R,int ldr,T*d_work,int ldwork)
+ *       TallShinnyQR.h:86-87, instantiated for float/double at :150-153
+ *   template<T> void qr(int m,int n,T*A,int lda,T*R,int ldr,T*d_work,int ldwork)
+ *       block_QR.h:72-73, instantiated for float/double at :96-99
+ * The reference returns void, asserts on bad sizes (TallShinnyQR.h:92-93,
+ * :109, :129; block_QR.h:78-79) and prints "not supported size" then returns
+ * (TallShinnyQR.h:100-103); here those become TSQR_ERR_INVALID_ARG and
+ * TSQR_ERR_UNSUPPORTED.
+ */
+#ifndef TSQR_GB300_H
+#define TSQR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tsqr_status {
+    TSQR_OK = 0,
+    TSQR_ERR_INVALID_ARG = 1,   /* bad m, n, lda, ldr, null pointer, m < n  */
+    TSQR_ERR_UNSUPPORTED = 2,   /* size or option this build does not cover */
+    TSQR_ERR_WORKSPACE = 3,     /* workspace pointer null or too small      */
+    TSQR_ERR_CUDA = 4,          /* a CUDA runtime call or launch failed     */
+    TSQR_ERR_NO_DEVICE = 5      /* no CUDA device / wrong architecture      */
+} tsqr_status;
+
+/* Arithmetic of the bulk reflector applications. */
+typedef enum tsqr_precision {
+    TSQR_PRECISION_PLAIN = 0,   /* working precision on CUDA cores (FP32 or FP64) */
+    TSQR_PRECISION_TF32X3 = 1,  /* FP32 entry points only: tcgen05 TF32 hi/lo
+                                   3-product split, FP32 accumulation in TMEM  */
+    TSQR_PRECISION_BF16X3 = 2   /* FP32 entry points only: tcgen05 BF16 hi/lo
+                                   3-product split, FP32 accumulation in TMEM  */
+} tsqr_precision;
+
+typedef struct tsqr_opts {
+    int precision;   /* tsqr_precision; ignored (always PLAIN) for FP64     */
+    int reorth;      /* qr only: 1 = second Gram-Schmidt projection (CGS2)  */
+    int panel;       /* qr only: panel width at which recursion stops, 0 = 32
+                        (the reference's N_B, block_QR.h:5)                 */
+    int reserved[5]; /* must be zero                                        */
+} tsqr_opts;
+
+/* Workspace bytes an ex call needs for an m x n problem of element size
+ * elem_bytes (4 or 8).  Returns 0 for sizes the library rejects. */
+size_t tsqr_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opts* opts);
+size_t qr_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opts* opts);
+
+/* TSQR: replaces tsqr<float>/tsqr<double> (TallShinnyQR.h:86-153).
+ * Any n >= 1 up to 64 (FP32) or 32 (FP64), any m >= n. */
+tsqr_status tsqr_s_ex(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr,
+                      void* work, size_t work_bytes, const tsqr_opts* opts, void* stream);
+tsqr_status tsqr_d_ex(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr,
+                      void* work, size_t work_bytes, const tsqr_opts* opts, void* stream);
+
+/* Recursive blocked QR: replaces qr<float>/qr<double> (block_QR.h:72-99):
+ * qr(A1); R12 = A1^T A2; A2 -= A1 R12; qr(A2), TSQR panels at the leaves. */
+tsqr_status qr_s_ex(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr,
+                    void* work, size_t work_bytes, const tsqr_opts* opts, void* stream);
+tsqr_status qr_d_ex(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr,
+                    void* work, size_t work_bytes, const tsqr_opts* opts, void* stream);
+
+/* Reference-signature forms (TallShinnyQR.h:87, block_QR.h:73): int sizes,
+ * the caller's d_work of ldwork*n elements, legacy default stream, PLAIN
+ * precision.  When d_work is smaller than the workspace this library needs,
+ * a per-device buffer cached inside the library is used instead. */
+tsqr_status tsqr_float(int m, int n, float* A, int lda, float* R, int ldr, float* d_work, int ldwork);
+tsqr_status tsqr_double(int m, int n, double* A, int lda, double* R, int ldr, double* d_work, int ldwork);
+tsqr_status qr_float(int m, int n, float* A, int lda, float* R, int ldr, float* d_work, int ldwork);
+tsqr_status qr_double(int m, int n, double* A, int lda, double* R, int ldr, double* d_work, int ldwork);
+
+/* Batched TSQR: `count` independent problems of uneven heights m[i] and
+ * widths n[i] (FP32, n[i] <= 64), factored by one persistent launch.  The
+ * pointer/size arrays are HOST arrays; A[i], R[i] are device pointers.  No
+ * counterpart in the reference (which factors one matrix per call). */
+size_t tsqr_batched_workspace_bytes(int count, const int64_t* m, const int64_t* n);
+tsqr_status tsqr_batched_s(int count, float* const* A, const int64_t* m, const int64_t* n,
+                           const int64_t* lda, float* const* R, const int64_t* ldr,
+                           void* work, size_t work_bytes, const tsqr_opts* opts, void* stream);
+
+/* Instrumentation (no counterpart in the reference): runs tsqr (kind 0) or
+ * qr (kind 1) exactly as the _ex entry points do, recording a CUDA event on
+ * `stream` before the first and after every kernel launch; synchronizes on
+ * the last event and writes each launch's device time in ms and its tag
+ * (kind*1000 + tree level; kinds 1 factor, 2 apply, 3-6 blocked-QR GEMM
+ * steps, 7 tensor-core kernels, 8 batched) to launch_ms / launch_tag. */
+tsqr_status tsqr_profile(int kind, int elem_bytes, int64_t m, int64_t n, void* A, int64_t lda, void* R,
+                         int64_t ldr, void* work, size_t work_bytes, const tsqr_opts* opts, void* stream,
+                         float* launch_ms, int* launch_tag, int max_launch, int* n_launch);
+
+/* Human-readable text of a status; never NULL. */
+const char* tsqr_status_string(tsqr_status s);
+
+/* Library version, e.g. "0.1.0". */
+const char* tsqr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TSQR_GB300_H */

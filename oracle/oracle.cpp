@@ -1,0 +1,548 @@
+// oracle.cpp -- CPU restatement of dajunHuang/tsqr's tall-skinny QR path.
+//
+// TEST INFRASTRUCTURE ONLY.  Nothing in the tsqr_gb300 product links, loads
+// or calls this file; only tests/, the smoke check and the CPU-baseline leg
+// of bench.py use it, as the checker.
+//
+// Contents (each function cites the reference file:line it restates):
+//   * orc_fill_uniform_{f,d}   the reference's seeded input stream
+//                              (test_tsqr.cu:24-28, test_qr.cu:24-28)
+//   * orc_tile_qr_{f,d}        Householder QR of one tile with explicit Q,
+//                              the reference's reflector convention
+//                              (kernelQR.h:101-157, :203-220, :227-275)
+//   * orc_ref_tsqr_{f,d}       the reference TSQR schedule: 128-row tiles,
+//                              reduction tree, Q back-propagation, 2-level
+//                              chunking (TallShinnyQR.h:86-148,
+//                              kernelQR.h:299-497, TallShinnyQR.h:11-74)
+//   * orc_ref_qr_{f,d}         recursive block Gram-Schmidt over TSQR
+//                              panels (block_QR.h:72-95, :7-60)
+//   * orc_householder_qr_d     FP64 column Householder QR (geqr2 + org2r
+//                              semantics, same reflector sign convention):
+//                              the FP64 truth every result is measured against
+//   * orc_metrics_{f,d}        backward error / orthogonality in FP64, in
+//                              Frobenius norm and in the reference's
+//                              spectral-norm form (utils.h:317-381)
+//   * orc_sign_fix_{f,d}       diag(R) >= 0 normalisation (flip row i of R
+//                              and column i of Q)
+//
+// Deviations from the reference, all deliberate and documented:
+//   * a column whose norm below the diagonal is exactly zero gets the
+//     identity reflector; the reference divides by zero there
+//     (kernelQR.h:126) and produces NaN;
+//   * the FP32 restatement sums dot products in plain sequential order;
+//     the reference sums per-lane partials then a 5-step xor butterfly
+//     (kernelQR.h:30-36), so FP32 results agree to rounding, not bitwise.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+enum { ORC_OK = 0, ORC_INVALID = 1, ORC_UNSUPPORTED = 2 };
+
+// ---------------------------------------------------------------------------
+// Householder QR of one h x n tile, reference convention.
+// kernelQR.h:101-157: for column j, with x = A(j:h, j):
+//   u = x / ||x||;  R_jj = -sign(u_1) ||x||;  u_1 += sign(u_1);
+//   u /= sqrt(|u_1|)            => H_j = I - u u^T with ||u||^2 = 2.
+// kernelQR.h:163-196: trailing columns x_c -= (u^T x_c) u over rows >= j.
+// kernelQR.h:203-220: R = strict upper part + RR on the diagonal, zero below.
+// kernelQR.h:227-275: Q(:, c) = H_0 H_1 ... H_{n-1} e_c (applied from
+//   H_{n-1} down to H_0, skipping H_j for j > c, which leave e_c unchanged).
+// Q (h x n, ldq) may alias A when ldq == lda.
+// ---------------------------------------------------------------------------
+template <typename T>
+void tile_qr(int64_t h, int64_t n, const T* A, int64_t lda, T* Q, int64_t ldq,
+             T* R, int64_t ldr) {
+    std::vector<T> W((size_t)h * n);
+    for (int64_t c = 0; c < n; ++c)
+        for (int64_t i = 0; i < h; ++i) W[i + c * h] = A[i + c * lda];
+    std::vector<T> rr(n, T(0));
+    const int64_t kmax = std::min(h, n);
+    for (int64_t j = 0; j < n; ++j) {
+        T* u = &W[j * h];
+        if (j >= h) {  // no rows left at or below the diagonal
+            rr[j] = T(0);
+            continue;
+        }
+        T nu = 0;
+        for (int64_t i = j; i < h; ++i) nu += u[i] * u[i];
+        T norm_x = std::sqrt(nu);
+        if (norm_x == T(0)) {  // deviation: identity reflector
+            rr[j] = T(0);
+            for (int64_t i = j; i < h; ++i) u[i] = T(0);
+            continue;
+        }
+        T scale = T(1.0 / norm_x);
+        for (int64_t i = j; i < h; ++i) u[i] *= scale;
+        T u1 = u[j];
+        u[j] += (u1 >= 0) ? T(1) : T(-1);
+        rr[j] = (u1 >= 0) ? -norm_x : norm_x;
+        scale = T(1) / std::sqrt(std::fabs(u[j]));
+        for (int64_t i = j; i < h; ++i) u[i] *= scale;
+        for (int64_t c = j + 1; c < n; ++c) {
+            T* x = &W[c * h];
+            T d = 0;
+            for (int64_t i = j; i < h; ++i) d += u[i] * x[i];
+            for (int64_t i = j; i < h; ++i) x[i] -= d * u[i];
+        }
+    }
+    (void)kmax;
+    // R extraction; zero the strict upper part so columns hold only u_j.
+    for (int64_t c = 0; c < n; ++c) {
+        for (int64_t r = 0; r < n; ++r) {
+            if (r < c) {
+                R[r + c * ldr] = (r < h) ? W[r + c * h] : T(0);
+                if (r < h) W[r + c * h] = T(0);
+            } else if (r > c) {
+                R[r + c * ldr] = T(0);
+            } else {
+                R[c + c * ldr] = rr[c];
+            }
+        }
+    }
+    // Explicit Q, one column at a time.
+    std::vector<T> q(h);
+    for (int64_t c = 0; c < n; ++c) {
+        for (int64_t i = 0; i < h; ++i) q[i] = (i == c) ? T(1) : T(0);
+        for (int64_t j = n - 1; j >= 0; --j) {
+            if (c < j || j >= h) continue;
+            const T* u = &W[j * h];
+            T d = 0;
+            for (int64_t i = 0; i < h; ++i) d += u[i] * q[i];
+            for (int64_t i = 0; i < h; ++i) q[i] -= d * u[i];
+        }
+        for (int64_t i = 0; i < h; ++i) Q[i + c * ldq] = q[i];
+    }
+}
+
+// C(h x n) = A(h x n) * B(n x n), sequential k sum: kernelQR.h:38-59 and
+// TallShinnyQR.h:43-47 use this order.
+template <typename T>
+void small_gemm(int64_t h, int64_t n, const T* A, int64_t lda, const T* B,
+                int64_t ldb, T* C, int64_t ldc) {
+    for (int64_t c = 0; c < n; ++c)
+        for (int64_t i = 0; i < h; ++i) {
+            T s = 0;
+            for (int64_t k = 0; k < n; ++k) s += A[i + k * lda] * B[k + c * ldb];
+            C[i + c * ldc] = s;
+        }
+}
+
+// One chunk of the reference's persistent kernel (kernelQR.h:321-496):
+// up-sweep over levels of bs-row tiles while the level height exceeds n (at
+// least one level, kernelQR.h:341-342); R of each tile stacked into the next
+// level; the single-tile top level writes R out; down-sweep multiplies each
+// tile's explicit Q by the n x n block of the finished level above
+// (kernelQR.h:397-492).
+template <typename T>
+void ref_tsqr_chunk(int64_t h0, int64_t n, T* A, int64_t lda, T* Rout,
+                    int64_t ldr, int64_t bs, bool parallel_tiles) {
+    struct Level {
+        int64_t h;
+        std::vector<T> q;  // explicit tile Q's, h x n, ld = h
+    };
+    std::vector<Level> levels;
+    std::vector<T> cur((size_t)h0 * n);
+    for (int64_t c = 0; c < n; ++c)
+        std::memcpy(&cur[c * h0], &A[c * lda], sizeof(T) * h0);
+    int64_t h = h0;
+    while (h > n || levels.empty()) {
+        int64_t ntiles = (h + bs - 1) / bs;
+        bool top = (h <= bs);
+        int64_t hn = ntiles * n;
+        Level L;
+        L.h = h;
+        L.q.assign((size_t)h * n, T(0));
+        std::vector<T> next(top ? 0 : (size_t)hn * n);
+#pragma omp parallel for schedule(dynamic) if (parallel_tiles && ntiles > 1)
+        for (int64_t t = 0; t < ntiles; ++t) {
+            int64_t r0 = t * bs, hb = std::min(bs, h - r0);
+            std::vector<T> Rt((size_t)n * n);
+            tile_qr<T>(hb, n, &cur[r0], h, &L.q[r0], h, Rt.data(), n);
+            if (top) {
+                for (int64_t c = 0; c < n; ++c)
+                    for (int64_t r = 0; r < n; ++r) Rout[r + c * ldr] = Rt[r + c * n];
+            } else {
+                for (int64_t c = 0; c < n; ++c)
+                    for (int64_t r = 0; r < n; ++r) next[t * n + r + c * hn] = Rt[r + c * n];
+            }
+        }
+        levels.push_back(std::move(L));
+        if (top) break;
+        cur.swap(next);
+        h = hn;
+    }
+    // Down-sweep: the top level's Q is final; each lower level multiplies.
+    std::vector<T> above = levels.back().q;
+    for (int64_t l = (int64_t)levels.size() - 2; l >= 0; --l) {
+        const Level& L = levels[l];
+        int64_t hl = L.h, ntiles = (hl + bs - 1) / bs, ha = ntiles * n;
+        std::vector<T> fin((size_t)hl * n);
+#pragma omp parallel for schedule(static) if (parallel_tiles && ntiles > 1)
+        for (int64_t t = 0; t < ntiles; ++t) {
+            int64_t r0 = t * bs, hb = std::min(bs, hl - r0);
+            small_gemm<T>(hb, n, &L.q[r0], hl, &above[t * n], ha, &fin[r0], hl);
+        }
+        above.swap(fin);
+    }
+    for (int64_t c = 0; c < n; ++c)
+        std::memcpy(&A[c * lda], &above[c * h0], sizeof(T) * h0);
+}
+
+// Host schedule of tsqr<T> (TallShinnyQR.h:86-148): size guard (:100-103),
+// 1-launch case (:128-148) or chunk loop + TSQR of the stacked chunk R's +
+// in-place fix-up A_g <- A_g * Q2_g (:108-127).  num_sm and bs stand for the
+// reference's NUM_SM and BLOCK_SIZE macros (kernelQR.h:3-4).
+template <typename T>
+int ref_tsqr(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr,
+             int64_t num_sm, int64_t bs) {
+    if (m < n || n < 1 || lda < m || ldr < n || num_sm < 1 || bs < 1) return ORC_INVALID;
+    if (bs % n != 0) return ORC_UNSUPPORTED;                   // TallShinnyQR.h:93
+    int64_t max_grid = num_sm * bs;
+    if (m > (max_grid / n) * max_grid) return ORC_UNSUPPORTED;  // :100-103
+    int64_t grid_num = (m + max_grid - 1) / max_grid;
+    if (grid_num > 1) {
+        if ((m % max_grid) % n != 0) return ORC_UNSUPPORTED;    // :109
+        int64_t hs = grid_num * n;
+        std::vector<T> W1((size_t)hs * n);
+#pragma omp parallel for schedule(dynamic)
+        for (int64_t g = 0; g < grid_num; ++g) {
+            int64_t r0 = g * max_grid, hg = std::min(max_grid, m - r0);
+            ref_tsqr_chunk<T>(hg, n, A + r0, lda, &W1[g * n], hs, bs, false);
+        }
+        ref_tsqr_chunk<T>(hs, n, W1.data(), hs, R, ldr, bs, false);
+#pragma omp parallel for schedule(dynamic)
+        for (int64_t g = 0; g < grid_num; ++g) {
+            int64_t r0 = g * max_grid, hg = std::min(max_grid, m - r0);
+            std::vector<T> tmp((size_t)hg * n);
+            small_gemm<T>(hg, n, A + r0, lda, &W1[g * n], hs, tmp.data(), hg);
+            for (int64_t c = 0; c < n; ++c)
+                std::memcpy(A + r0 + c * lda, &tmp[c * hg], sizeof(T) * hg);
+        }
+    } else {
+        if ((m % bs) % n != 0) return ORC_UNSUPPORTED;          // :129
+        ref_tsqr_chunk<T>(m, n, A, lda, R, ldr, bs, true);
+    }
+    return ORC_OK;
+}
+
+// Recursive block classical Gram-Schmidt with TSQR panels (block_QR.h:72-95):
+// qr(A1); R12 = A1^T A2 (block_QR.h:40-58, sequential sum over rows);
+// A2 -= A1 R12 (block_QR.h:21-39); qr(A2).  The reference leaves the R21
+// block unwritten; this restatement writes zeros there.
+template <typename T>
+int ref_qr(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr,
+           int64_t num_sm, int64_t bs, int64_t nb) {
+    if (n <= nb) return ref_tsqr<T>(m, n, A, lda, R, ldr, num_sm, bs);
+    if (n % 2 != 0 || (n / 2) % nb != 0) return ORC_UNSUPPORTED;  // block_QR.h:78-79
+    int64_t n1 = n / 2;
+    T* A1 = A;
+    T* A2 = A + n1 * lda;
+    T* R11 = R;
+    T* R12 = R + n1 * ldr;
+    T* R22 = R + n1 * ldr + n1;
+    int rc = ref_qr<T>(m, n1, A1, lda, R11, ldr, num_sm, bs, nb);
+    if (rc) return rc;
+#pragma omp parallel for collapse(2)
+    for (int64_t c = 0; c < n1; ++c)
+        for (int64_t r = 0; r < n1; ++r) {
+            T s = 0;
+            for (int64_t i = 0; i < m; ++i) s += A1[i + r * lda] * A2[i + c * lda];
+            R12[r + c * ldr] = s;
+        }
+    for (int64_t c = 0; c < n1; ++c)
+        for (int64_t r = 0; r < n1; ++r) R[n1 + r + c * ldr] = T(0);
+#pragma omp parallel for
+    for (int64_t i = 0; i < m; ++i)
+        for (int64_t c = 0; c < n1; ++c) {
+            T s = 0;
+            for (int64_t k = 0; k < n1; ++k) s += A1[i + k * lda] * R12[k + c * ldr];
+            A2[i + c * lda] = -s + A2[i + c * lda];
+        }
+    return ref_qr<T>(m, n1, A2, lda, R22, ldr, num_sm, bs, nb);
+}
+
+// FP64 column Householder QR with explicit thin Q (geqr2 + org2r semantics),
+// the same reflector convention as kernelQR.h:137-156, written over
+// OpenMP-parallel row reductions so that 4M-row inputs finish in seconds.
+int householder_qr_d(int64_t m, int64_t n, double* A, int64_t lda, double* R,
+                     int64_t ldr) {
+    if (m < n || n < 1 || lda < m || ldr < n) return ORC_INVALID;
+    std::vector<double> rr(n);
+    std::vector<double> d(n);
+    for (int64_t j = 0; j < n; ++j) {
+        double* u = A + j * lda;
+        double nu = 0;
+#pragma omp parallel for reduction(+ : nu)
+        for (int64_t i = j; i < m; ++i) nu += u[i] * u[i];
+        double nx = std::sqrt(nu);
+        if (nx == 0.0) {
+            rr[j] = 0.0;
+            continue;  // u stays zero below the diagonal: identity reflector
+        }
+        double u1 = u[j] / nx;
+        rr[j] = (u1 >= 0) ? -nx : nx;
+        double s1 = 1.0 / nx;
+        double top = u1 + ((u1 >= 0) ? 1.0 : -1.0);
+        double s2 = 1.0 / std::sqrt(std::fabs(top));
+#pragma omp parallel for
+        for (int64_t i = j + 1; i < m; ++i) u[i] = u[i] * s1 * s2;
+        u[j] = top * s2;
+        int64_t k = n - j - 1;
+        if (k > 0) {
+            std::fill(d.begin(), d.end(), 0.0);
+#pragma omp parallel
+            {
+                std::vector<double> dl(k, 0.0);
+#pragma omp for nowait
+                for (int64_t i = j; i < m; ++i) {
+                    double ui = u[i];
+                    for (int64_t c = 0; c < k; ++c) dl[c] += ui * A[i + (j + 1 + c) * lda];
+                }
+#pragma omp critical
+                for (int64_t c = 0; c < k; ++c) d[c] += dl[c];
+            }
+#pragma omp parallel for
+            for (int64_t i = j; i < m; ++i) {
+                double ui = u[i];
+                for (int64_t c = 0; c < k; ++c) A[i + (j + 1 + c) * lda] -= d[c] * ui;
+            }
+        }
+    }
+    for (int64_t c = 0; c < n; ++c)
+        for (int64_t r = 0; r < n; ++r) {
+            if (r < c) {
+                R[r + c * ldr] = A[r + c * lda];
+                A[r + c * lda] = 0.0;
+            } else if (r > c) {
+                R[r + c * ldr] = 0.0;
+            } else {
+                R[c + c * ldr] = rr[c];
+            }
+        }
+    // Explicit Q: apply H_{n-1} ... H_0 to [I; 0], all columns together.
+    std::vector<double> Q((size_t)m * n, 0.0);
+    for (int64_t c = 0; c < n; ++c) Q[c + c * m] = 1.0;
+    for (int64_t j = n - 1; j >= 0; --j) {
+        const double* u = A + j * lda;
+        int64_t k = n - j;  // columns j..n-1 can be touched
+        std::fill(d.begin(), d.end(), 0.0);
+#pragma omp parallel
+        {
+            std::vector<double> dl(k, 0.0);
+#pragma omp for nowait
+            for (int64_t i = j; i < m; ++i) {
+                double ui = u[i];
+                for (int64_t c = 0; c < k; ++c) dl[c] += ui * Q[i + (j + c) * m];
+            }
+#pragma omp critical
+            for (int64_t c = 0; c < k; ++c) d[c] += dl[c];
+        }
+#pragma omp parallel for
+        for (int64_t i = j; i < m; ++i) {
+            double ui = u[i];
+            for (int64_t c = 0; c < k; ++c) Q[i + (j + c) * m] -= d[c] * ui;
+        }
+    }
+#pragma omp parallel for
+    for (int64_t c = 0; c < n; ++c)
+        std::memcpy(A + c * lda, &Q[c * m], sizeof(double) * m);
+    return ORC_OK;
+}
+
+// Largest eigenvalue of a symmetric n x n matrix (cyclic Jacobi), used for
+// spectral norms ||E||_2 = sqrt(lambda_max(E^T E)).
+double sym_lambda_max(std::vector<double> S, int64_t n) {
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0, tot = 0;
+        for (int64_t p = 0; p < n; ++p)
+            for (int64_t q = 0; q < n; ++q) {
+                double v = S[p + q * n] * S[p + q * n];
+                tot += v;
+                if (p != q) off += v;
+            }
+        if (off <= 1e-30 * tot || off == 0) break;
+        for (int64_t p = 0; p < n - 1; ++p)
+            for (int64_t q = p + 1; q < n; ++q) {
+                double apq = S[p + q * n];
+                if (apq == 0) continue;
+                double app = S[p + p * n], aqq = S[q + q * n];
+                double theta = (aqq - app) / (2 * apq);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
+                double c = 1 / std::sqrt(t * t + 1), s = t * c;
+                for (int64_t k = 0; k < n; ++k) {
+                    double skp = S[k + p * n], skq = S[k + q * n];
+                    S[k + p * n] = c * skp - s * skq;
+                    S[k + q * n] = s * skp + c * skq;
+                }
+                for (int64_t k = 0; k < n; ++k) {
+                    double spk = S[p + k * n], sqk = S[q + k * n];
+                    S[p + k * n] = c * spk - s * sqk;
+                    S[q + k * n] = s * spk + c * sqk;
+                }
+            }
+    }
+    double mx = 0;
+    for (int64_t i = 0; i < n; ++i) mx = std::max(mx, S[i + i * n]);
+    return mx;
+}
+
+// Gram matrix G = X^T X (n x n) in FP64 of an m x n matrix given by a
+// row functor, OpenMP over rows.
+template <typename F>
+std::vector<double> gram(int64_t m, int64_t n, F row) {
+    std::vector<double> G((size_t)n * n, 0.0);
+#pragma omp parallel
+    {
+        std::vector<double> Gl((size_t)n * n, 0.0), x(n);
+#pragma omp for nowait
+        for (int64_t i = 0; i < m; ++i) {
+            row(i, x.data());
+            for (int64_t c = 0; c < n; ++c)
+                for (int64_t r = 0; r <= c; ++r) Gl[r + c * n] += x[r] * x[c];
+        }
+#pragma omp critical
+        for (size_t k = 0; k < Gl.size(); ++k) G[k] += Gl[k];
+    }
+    for (int64_t c = 0; c < n; ++c)
+        for (int64_t r = c + 1; r < n; ++r) G[r + c * n] = G[c + r * n];
+    return G;
+}
+
+// out[0] = ||A - QR||_F / ||A||_F           (Frobenius backward error)
+// out[1] = ||Q^T Q - I||_F                   (Frobenius orthogonality)
+// out[2] = ||A - QR||_2 / ||A||_2            (utils.h:353, first figure)
+// out[3] = ||I - Q^T Q||_2 / n               (utils.h:353-354, second figure)
+// All in FP64 regardless of T.  R is read as a full n x n matrix, as the
+// reference's checker does (utils.h:384-385).
+template <typename T>
+void metrics(int64_t m, int64_t n, const T* A0, int64_t lda0, const T* Q,
+             int64_t ldq, const T* R, int64_t ldr, double* out) {
+    std::vector<double> Rd((size_t)n * n);
+    for (int64_t c = 0; c < n; ++c)
+        for (int64_t r = 0; r < n; ++r) Rd[r + c * n] = (double)R[r + c * ldr];
+    auto erow = [&](int64_t i, double* x) {
+        for (int64_t c = 0; c < n; ++c) {
+            double s = 0;
+            for (int64_t k = 0; k < n; ++k) s += (double)Q[i + k * ldq] * Rd[k + c * n];
+            x[c] = (double)A0[i + c * lda0] - s;
+        }
+    };
+    auto arow = [&](int64_t i, double* x) {
+        for (int64_t c = 0; c < n; ++c) x[c] = (double)A0[i + c * lda0];
+    };
+    auto qrow = [&](int64_t i, double* x) {
+        for (int64_t c = 0; c < n; ++c) x[c] = (double)Q[i + c * ldq];
+    };
+    std::vector<double> GE = gram(m, n, erow);
+    std::vector<double> GA = gram(m, n, arow);
+    std::vector<double> GQ = gram(m, n, qrow);
+    double fe = 0, fa = 0, fo = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        fe += GE[i + i * n];
+        fa += GA[i + i * n];
+    }
+    for (int64_t c = 0; c < n; ++c)
+        for (int64_t r = 0; r < n; ++r) {
+            double v = GQ[r + c * n] - (r == c ? 1.0 : 0.0);
+            GQ[r + c * n] = v;
+            fo += v * v;
+        }
+    out[0] = (fa > 0) ? std::sqrt(fe / fa) : std::sqrt(fe);
+    out[1] = std::sqrt(fo);
+    double le = sym_lambda_max(GE, n), la = sym_lambda_max(GA, n);
+    out[2] = (la > 0) ? std::sqrt(std::max(le, 0.0) / la) : std::sqrt(std::max(le, 0.0));
+    // ||I - Q^T Q||_2 of a symmetric matrix = max |eigenvalue|.
+    std::vector<double> sq((size_t)n * n, 0.0);
+    for (int64_t c = 0; c < n; ++c)
+        for (int64_t r = 0; r < n; ++r) {
+            double s = 0;
+            for (int64_t k = 0; k < n; ++k) s += GQ[r + k * n] * GQ[k + c * n];
+            sq[r + c * n] = s;
+        }
+    out[3] = std::sqrt(std::max(sym_lambda_max(sq, n), 0.0)) / (double)n;
+}
+
+template <typename T>
+void sign_fix(int64_t m, int64_t n, T* Q, int64_t ldq, T* R, int64_t ldr) {
+    for (int64_t j = 0; j < n; ++j) {
+        if (R[j + j * ldr] < T(0)) {
+            for (int64_t c = 0; c < n; ++c) R[j + c * ldr] = -R[j + c * ldr];
+            for (int64_t i = 0; i < m; ++i) Q[i + j * ldq] = -Q[i + j * ldq];
+        }
+    }
+}
+
+template <typename T>
+void fill_uniform(T* a, int64_t count, unsigned seed) {
+    // test_tsqr.cu:24-28: std::default_random_engine eng(0U);
+    // std::uniform_real_distribution<T> dis(-1.0f, 1.0f); std::generate.
+    std::default_random_engine eng(seed);
+    std::uniform_real_distribution<T> dis(-1.0f, 1.0f);
+    for (int64_t i = 0; i < count; ++i) a[i] = dis(eng);
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_fill_uniform_f(float* a, int64_t count, unsigned seed) { fill_uniform<float>(a, count, seed); }
+void orc_fill_uniform_d(double* a, int64_t count, unsigned seed) { fill_uniform<double>(a, count, seed); }
+
+int orc_tile_qr_f(int64_t h, int64_t n, const float* A, int64_t lda, float* Q, int64_t ldq, float* R, int64_t ldr) {
+    if (h < 1 || n < 1) return ORC_INVALID;
+    tile_qr<float>(h, n, A, lda, Q, ldq, R, ldr);
+    return ORC_OK;
+}
+int orc_tile_qr_d(int64_t h, int64_t n, const double* A, int64_t lda, double* Q, int64_t ldq, double* R, int64_t ldr) {
+    if (h < 1 || n < 1) return ORC_INVALID;
+    tile_qr<double>(h, n, A, lda, Q, ldq, R, ldr);
+    return ORC_OK;
+}
+
+int orc_ref_tsqr_f(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, int64_t num_sm, int64_t bs) {
+    return ref_tsqr<float>(m, n, A, lda, R, ldr, num_sm, bs);
+}
+int orc_ref_tsqr_d(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr, int64_t num_sm, int64_t bs) {
+    return ref_tsqr<double>(m, n, A, lda, R, ldr, num_sm, bs);
+}
+int orc_ref_qr_f(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, int64_t num_sm, int64_t bs, int64_t nb) {
+    return ref_qr<float>(m, n, A, lda, R, ldr, num_sm, bs, nb);
+}
+int orc_ref_qr_d(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr, int64_t num_sm, int64_t bs, int64_t nb) {
+    return ref_qr<double>(m, n, A, lda, R, ldr, num_sm, bs, nb);
+}
+int orc_householder_qr_d(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr) {
+    return householder_qr_d(m, n, A, lda, R, ldr);
+}
+void orc_metrics_f(int64_t m, int64_t n, const float* A0, int64_t lda0, const float* Q, int64_t ldq, const float* R, int64_t ldr, double* out) {
+    metrics<float>(m, n, A0, lda0, Q, ldq, R, ldr, out);
+}
+void orc_metrics_d(int64_t m, int64_t n, const double* A0, int64_t lda0, const double* Q, int64_t ldq, const double* R, int64_t ldr, double* out) {
+    metrics<double>(m, n, A0, lda0, Q, ldq, R, ldr, out);
+}
+void orc_sign_fix_f(int64_t m, int64_t n, float* Q, int64_t ldq, float* R, int64_t ldr) { sign_fix<float>(m, n, Q, ldq, R, ldr); }
+void orc_sign_fix_d(int64_t m, int64_t n, double* Q, int64_t ldq, double* R, int64_t ldr) { sign_fix<double>(m, n, Q, ldq, R, ldr); }
+int orc_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+void orc_set_num_threads(int t) {
+#ifdef _OPENMP
+    if (t > 0) omp_set_num_threads(t);
+#else
+    (void)t;
+#endif
+}
+
+}  // extern "C"

@@ -1,0 +1,84 @@
+"""CPU tests of the drop-in boundary: the C-ABI library loads, exports every
+symbol include/tsqr_gb300.h declares, and rejects bad arguments before any
+CUDA call (the reference asserts or prints instead: TallShinnyQR.h:92-109,
+block_QR.h:78-79).  No compute call is made here."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "tsqr_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[a-z_][a-z0-9_]*\s*\*?\s+([a-z_][a-z0-9_]*)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_the_reference_entry_points():
+    names = declared_functions()
+    for n in ("tsqr_float", "tsqr_double", "qr_float", "qr_double", "tsqr_s_ex", "tsqr_d_ex", "qr_s_ex",
+              "qr_d_ex", "tsqr_workspace_bytes", "qr_workspace_bytes", "tsqr_batched_s", "tsqr_status_string"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(tg):
+    L = ctypes.CDLL(tg.library_path())
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+    assert set(declared_functions()) <= set(tg.EXPORTS)
+
+
+def test_status_strings(tg):
+    for s in range(6):
+        assert tg.lib().tsqr_status_string(s)
+    assert tg.lib().tsqr_version().decode().count(".") == 2
+
+
+@pytest.mark.parametrize("m,n,lda,ldr,st", [
+    (0, 1, 1, 1, 1), (10, 0, 10, 1, 1), (10, 20, 10, 20, 1),   # m < n rejected (TallShinnyQR.h:92)
+    (100, 8, 99, 8, 1), (100, 8, 100, 7, 1), (100, 65, 100, 65, 2),
+])
+def test_tsqr_argument_checks_need_no_gpu(tg, m, n, lda, ldr, st):
+    o = tg.Opts()
+    fake = ctypes.c_void_p(0x1000)
+    rc = tg.lib().tsqr_s_ex(m, n, fake, lda, fake, ldr, fake, 1 << 20, ctypes.byref(o), None)
+    assert rc == st
+
+
+def test_null_pointers_and_options_rejected(tg):
+    o = tg.Opts()
+    fake = ctypes.c_void_p(0x1000)
+    L = tg.lib()
+    assert L.tsqr_s_ex(64, 8, None, 64, fake, 8, fake, 1 << 20, ctypes.byref(o), None) == 1
+    assert L.tsqr_d_ex(64, 8, fake, 64, None, 8, fake, 1 << 20, ctypes.byref(o), None) == 1
+    o.reserved[0] = 7
+    assert L.qr_s_ex(64, 8, fake, 64, fake, 8, fake, 1 << 20, ctypes.byref(o), None) == 1
+    o = tg.Opts()
+    o.precision = 9
+    assert L.tsqr_s_ex(64, 8, fake, 64, fake, 8, fake, 1 << 20, ctypes.byref(o), None) == 1
+    assert L.tsqr_d_ex(64, 33, fake, 64, fake, 33, fake, 1 << 20, None, None) == 2  # FP64 n <= 32
+
+
+def test_workspace_too_small_is_reported(tg):
+    o = tg.Opts()
+    fake = ctypes.c_void_p(0x1000)
+    need = tg.lib().tsqr_workspace_bytes(1 << 20, 32, 4, ctypes.byref(o))
+    assert need > 0
+    assert tg.lib().tsqr_s_ex(1 << 20, 32, fake, 1 << 20, fake, 32, fake, need - 1, ctypes.byref(o), None) == 3
+    assert tg.lib().tsqr_s_ex(1 << 20, 32, fake, 1 << 20, fake, 32, None, need, ctypes.byref(o), None) == 3
+
+
+def test_workspace_sizes_are_small(tg):
+    # The R stack of the tree is the only workspace: n/B of A per level.
+    for n in (8, 16, 32, 64):
+        m = 4194304
+        ws = tg.workspace_bytes(m, n, "float32")
+        assert 0 < ws < 0.35 * m * n * 4
+    assert tg.workspace_bytes(100, 200, "float32") == 0        # m < n
+    assert tg.qr_workspace_bytes(27648, 128, "float64") > 0
+    assert tg.qr_workspace_bytes(27648, 128, "float64", reorth=True) > tg.qr_workspace_bytes(27648, 128, "float64")

@@ -1,0 +1,265 @@
+"""tsqr_gb300 -- tall-skinny QR for one GB300 GPU (sm_103a).
+
+Host-side mirror of the reference interface over the C ABI of
+``libtsqr_gb300.so`` (declared in include/tsqr_gb300.h):
+
+* ``tsqr(m, n, A, lda, R, ldr, d_work, ldwork, dtype)`` and
+  ``qr(...)``: the reference signatures (TallShinnyQR.h:86-87,
+  block_QR.h:72-73) on raw device pointers, legacy default stream;
+* ``tsqr_(A, ...)`` / ``qr_(...)``: the same on torch CUDA tensors holding
+  column-major matrices (shape (m, n), stride (1, lda)), on the current
+  stream, with the precision form selectable;
+* ``tsqr_batched_(As, ...)``: many uneven problems in one launch.
+
+There is no CPU fallback: if the shared library is missing or was built for
+another machine, importing the package raises.
+"""
+import ctypes
+import os
+
+__all__ = [
+    "TsqrError", "PLAIN", "TF32X3", "BF16X3", "lib", "library_path", "tsqr", "qr", "tsqr_", "qr_",
+    "tsqr_batched_", "profile_", "workspace_bytes", "qr_workspace_bytes", "empty_colmajor", "to_colmajor",
+]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(HERE, "_build", "libtsqr_gb300.so")
+
+PLAIN, TF32X3, BF16X3 = 0, 1, 2
+_PREC = {"plain": PLAIN, "tf32x3": TF32X3, "bf16x3": BF16X3, PLAIN: PLAIN, TF32X3: TF32X3, BF16X3: BF16X3}
+
+STATUS = {0: "TSQR_OK", 1: "TSQR_ERR_INVALID_ARG", 2: "TSQR_ERR_UNSUPPORTED", 3: "TSQR_ERR_WORKSPACE",
+          4: "TSQR_ERR_CUDA", 5: "TSQR_ERR_NO_DEVICE"}
+
+
+class TsqrError(RuntimeError):
+    def __init__(self, status, where=""):
+        self.status = status
+        super().__init__("%s: %s (%s)" % (where, STATUS.get(status, status), _status_text(status)))
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("reorth", ctypes.c_int), ("panel", ctypes.c_int),
+                ("reserved", ctypes.c_int * 5)]
+
+
+_i64 = ctypes.c_int64
+_p = ctypes.c_void_p
+_L = None
+
+# name -> (argtypes, restype); the full export list of include/tsqr_gb300.h
+EXPORTS = {
+    "tsqr_workspace_bytes": ([_i64, _i64, ctypes.c_int, ctypes.POINTER(Opts)], ctypes.c_size_t),
+    "qr_workspace_bytes": ([_i64, _i64, ctypes.c_int, ctypes.POINTER(Opts)], ctypes.c_size_t),
+    "tsqr_s_ex": ([_i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p], ctypes.c_int),
+    "tsqr_d_ex": ([_i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p], ctypes.c_int),
+    "qr_s_ex": ([_i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p], ctypes.c_int),
+    "qr_d_ex": ([_i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p], ctypes.c_int),
+    "tsqr_float": ([ctypes.c_int] * 2 + [_p, ctypes.c_int, _p, ctypes.c_int, _p, ctypes.c_int], ctypes.c_int),
+    "tsqr_double": ([ctypes.c_int] * 2 + [_p, ctypes.c_int, _p, ctypes.c_int, _p, ctypes.c_int], ctypes.c_int),
+    "qr_float": ([ctypes.c_int] * 2 + [_p, ctypes.c_int, _p, ctypes.c_int, _p, ctypes.c_int], ctypes.c_int),
+    "qr_double": ([ctypes.c_int] * 2 + [_p, ctypes.c_int, _p, ctypes.c_int, _p, ctypes.c_int], ctypes.c_int),
+    "tsqr_batched_workspace_bytes": ([ctypes.c_int, _p, _p], ctypes.c_size_t),
+    "tsqr_batched_s": ([ctypes.c_int, _p, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p],
+                       ctypes.c_int),
+    "tsqr_profile": ([ctypes.c_int, ctypes.c_int, _i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t,
+                      ctypes.POINTER(Opts), _p, _p, _p, ctypes.c_int, _p], ctypes.c_int),
+    "tsqr_status_string": ([ctypes.c_int], ctypes.c_char_p),
+    "tsqr_version": ([], ctypes.c_char_p),
+}
+
+
+def library_path():
+    return _LIB_PATH
+
+
+def lib():
+    """Load libtsqr_gb300.so (raises if it has not been built)."""
+    global _L
+    if _L is None:
+        if not os.path.exists(_LIB_PATH):
+            raise ImportError("libtsqr_gb300.so not built; run `python -c 'import __graft_entry__ as g; g.build()'`"
+                              " or `python tsqr_gb300/build.py`")
+        L = ctypes.CDLL(_LIB_PATH)
+        for name, (args, res) in EXPORTS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _L = L
+    return _L
+
+
+def _status_text(st):
+    try:
+        return lib().tsqr_status_string(int(st)).decode()
+    except Exception:  # pragma: no cover - library missing while formatting an error
+        return "?"
+
+
+def _check(st, where):
+    if st != 0:
+        raise TsqrError(st, where)
+
+
+def _opts(precision="plain", reorth=False, panel=0):
+    o = Opts()
+    o.precision = _PREC[precision]
+    o.reorth = 1 if reorth else 0
+    o.panel = int(panel)
+    return o
+
+
+def _elem(dtype):
+    import torch
+    if dtype in (torch.float32, "float32", "float", 4):
+        return 4
+    if dtype in (torch.float64, "float64", "double", 8):
+        return 8
+    raise TsqrError(1, "dtype %s" % (dtype,))
+
+
+def workspace_bytes(m, n, dtype, precision="plain"):
+    o = _opts(precision)
+    return int(lib().tsqr_workspace_bytes(m, n, _elem(dtype), ctypes.byref(o)))
+
+
+def qr_workspace_bytes(m, n, dtype, precision="plain", reorth=False, panel=0):
+    o = _opts(precision, reorth, panel)
+    return int(lib().qr_workspace_bytes(m, n, _elem(dtype), ctypes.byref(o)))
+
+
+# ---------------------------------------------------------------------------
+# Reference signatures on raw device pointers (TallShinnyQR.h:86-87,
+# block_QR.h:72-73).  dtype "float" or "double".
+# ---------------------------------------------------------------------------
+def tsqr(m, n, A, lda, R, ldr, d_work, ldwork, dtype="float"):
+    fn = lib().tsqr_float if _elem(dtype) == 4 else lib().tsqr_double
+    _check(fn(m, n, A, lda, R, ldr, d_work, ldwork), "tsqr")
+
+
+def qr(m, n, A, lda, R, ldr, d_work, ldwork, dtype="float"):
+    fn = lib().qr_float if _elem(dtype) == 4 else lib().qr_double
+    _check(fn(m, n, A, lda, R, ldr, d_work, ldwork), "qr")
+
+
+# ---------------------------------------------------------------------------
+# torch tensors
+# ---------------------------------------------------------------------------
+def empty_colmajor(m, n, dtype=None, device="cuda", ld=None):
+    """An (m, n) column-major tensor view with leading dimension ld >= m."""
+    import torch
+    ld = m if ld is None else ld
+    return torch.empty((n, ld), dtype=dtype or torch.float32, device=device).t()[:m]
+
+
+def to_colmajor(x):
+    """Column-major copy of a 2-D tensor (no copy if it already is one)."""
+    if x.dim() == 2 and x.stride(0) == 1 and x.stride(1) >= max(1, x.shape[0]):
+        return x
+    return x.t().contiguous().t()
+
+
+def _ld(x):
+    m, n = x.shape
+    if x.stride(0) != 1 or (n > 1 and x.stride(1) < m):
+        raise TsqrError(1, "matrix must be column-major (stride (1, ld>=m))")
+    return x.stride(1) if n > 1 else max(m, x.stride(1))
+
+
+def _stream_handle(stream):
+    import torch
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+
+
+def _work(nbytes, work, device):
+    import torch
+    if work is not None:
+        if work.numel() * work.element_size() < nbytes:
+            raise TsqrError(3, "workspace")
+        return work, work.numel() * work.element_size()
+    return torch.empty(max(nbytes, 1), dtype=torch.uint8, device=device), max(nbytes, 1)
+
+
+def tsqr_(A, R=None, precision="plain", work=None, stream=None):
+    """Factor the column-major m x n CUDA tensor A in place: A <- Q.
+    Returns R (n x n, column-major).  precision: "plain", "tf32x3",
+    "bf16x3" (the last two for float32 only)."""
+    import torch
+    m, n = A.shape
+    lda = _ld(A)
+    if R is None:
+        R = empty_colmajor(n, n, A.dtype, A.device)
+    ldr = _ld(R)
+    o = _opts(precision)
+    nbytes = int(lib().tsqr_workspace_bytes(m, n, A.element_size(), ctypes.byref(o)))
+    if nbytes == 0:
+        raise TsqrError(2, "tsqr_ workspace (m=%d n=%d)" % (m, n))
+    w, wb = _work(nbytes, work, A.device)
+    fn = lib().tsqr_s_ex if A.dtype == torch.float32 else lib().tsqr_d_ex
+    _check(fn(m, n, A.data_ptr(), lda, R.data_ptr(), ldr, w.data_ptr(), wb, ctypes.byref(o),
+              _stream_handle(stream)), "tsqr_")
+    return R
+
+
+def qr_(A, R=None, precision="plain", reorth=False, panel=0, work=None, stream=None):
+    """Recursive blocked QR of the column-major CUDA tensor A in place."""
+    import torch
+    m, n = A.shape
+    lda = _ld(A)
+    if R is None:
+        R = empty_colmajor(n, n, A.dtype, A.device)
+    ldr = _ld(R)
+    o = _opts(precision, reorth, panel)
+    nbytes = int(lib().qr_workspace_bytes(m, n, A.element_size(), ctypes.byref(o)))
+    if nbytes == 0:
+        raise TsqrError(2, "qr_ workspace (m=%d n=%d)" % (m, n))
+    w, wb = _work(nbytes, work, A.device)
+    fn = lib().qr_s_ex if A.dtype == torch.float32 else lib().qr_d_ex
+    _check(fn(m, n, A.data_ptr(), lda, R.data_ptr(), ldr, w.data_ptr(), wb, ctypes.byref(o),
+              _stream_handle(stream)), "qr_")
+    return R
+
+
+def profile_(kind, A, R, precision="plain", reorth=False, panel=0, work=None, stream=None, max_launch=512):
+    """Run tsqr_ (kind "tsqr") or qr_ (kind "qr") with per-launch device
+    timing.  Returns [(tag, ms), ...] in launch order; tag = kind*1000+level
+    (1 factor, 2 apply, 3 gemm_tn, 4 reduce, 5 gemm_nn, 6 axpy, 7 tcgen05,
+    8 batched)."""
+    m, n = A.shape
+    o = _opts(precision, reorth, panel)
+    k = 0 if kind == "tsqr" else 1
+    nbytes = (lib().tsqr_workspace_bytes if k == 0 else lib().qr_workspace_bytes)(m, n, A.element_size(),
+                                                                                 ctypes.byref(o))
+    w, wb = _work(int(nbytes), work, A.device)
+    ms = (ctypes.c_float * max_launch)()
+    tags = (ctypes.c_int * max_launch)()
+    cnt = ctypes.c_int(0)
+    _check(lib().tsqr_profile(k, A.element_size(), m, n, A.data_ptr(), _ld(A), R.data_ptr(), _ld(R), w.data_ptr(),
+                              wb, ctypes.byref(o), _stream_handle(stream), ms, tags, max_launch,
+                              ctypes.byref(cnt)), "profile_")
+    return [(tags[i], ms[i]) for i in range(cnt.value)]
+
+
+def tsqr_batched_(As, Rs=None, precision="plain", work=None, stream=None):
+    """Factor a list of column-major float32 CUDA tensors in one launch."""
+    import torch
+    count = len(As)
+    if Rs is None:
+        Rs = [empty_colmajor(a.shape[1], a.shape[1], a.dtype, a.device) for a in As]
+    i64 = ctypes.c_int64 * count
+    ptrs = ctypes.c_void_p * count
+    m = i64(*[a.shape[0] for a in As])
+    n = i64(*[a.shape[1] for a in As])
+    lda = i64(*[_ld(a) for a in As])
+    ldr = i64(*[_ld(r) for r in Rs])
+    Ap = ptrs(*[a.data_ptr() for a in As])
+    Rp = ptrs(*[r.data_ptr() for r in Rs])
+    nbytes = int(lib().tsqr_batched_workspace_bytes(count, m, n))
+    dev = As[0].device if count else torch.device("cuda")
+    w, wb = _work(nbytes, work, dev)
+    o = _opts(precision)
+    _check(lib().tsqr_batched_s(count, Ap, m, n, lda, Rp, ldr, w.data_ptr(), wb, ctypes.byref(o),
+                                _stream_handle(stream)), "tsqr_batched_")
+    return Rs

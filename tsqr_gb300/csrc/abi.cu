@@ -1,0 +1,196 @@
+// abi.cu -- extern "C" entry points of libtsqr_gb300.so.
+//
+// Argument checks replace the reference's host asserts and its silent
+// "not supported size" return (TallShinnyQR.h:92-93, :100-103, :109, :129;
+// block_QR.h:78-79): every rejected call returns a status and launches
+// nothing.
+#include <cuda_runtime.h>
+
+#include "../../include/tsqr_gb300.h"
+#include "internal.h"
+
+namespace {
+
+tsqr_opts opts_or_default(const tsqr_opts* o) {
+    tsqr_opts d = {};
+    return o ? *o : d;
+}
+
+template <typename T>
+int max_tsqr_n() {
+    return sizeof(T) == 4 ? 64 : 32;
+}
+
+template <typename T>
+tsqr_status check_common(int64_t m, int64_t n, const T* A, int64_t lda, const T* R, int64_t ldr,
+                         const tsqr_opts& o) {
+    if (m < 1 || n < 1 || m < n) return TSQR_ERR_INVALID_ARG;
+    if (lda < m || ldr < n) return TSQR_ERR_INVALID_ARG;
+    if (A == nullptr || R == nullptr) return TSQR_ERR_INVALID_ARG;
+    for (int i = 0; i < 5; ++i)
+        if (o.reserved[i] != 0) return TSQR_ERR_INVALID_ARG;
+    if (o.precision < TSQR_PRECISION_PLAIN || o.precision > TSQR_PRECISION_BF16X3) return TSQR_ERR_INVALID_ARG;
+    if (o.panel < 0 || o.reorth < 0 || o.reorth > 1) return TSQR_ERR_INVALID_ARG;
+    return TSQR_OK;
+}
+
+template <typename T>
+tsqr_status tsqr_ex(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
+                    const tsqr_opts* op, void* stream) {
+    const tsqr_opts o = opts_or_default(op);
+    tsqr_status st = check_common<T>(m, n, A, lda, R, ldr, o);
+    if (st != TSQR_OK) return st;
+    if (n > max_tsqr_n<T>()) return TSQR_ERR_UNSUPPORTED;
+    if (sizeof(T) == 8 || o.precision == TSQR_PRECISION_PLAIN)
+        return tsqr::tsqr_plain<T>(m, n, A, lda, R, ldr, work, work_bytes, (cudaStream_t)stream);
+    return TSQR_ERR_UNSUPPORTED;
+}
+
+template <typename T>
+tsqr_status qr_ex(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
+                  const tsqr_opts* op, void* stream) {
+    const tsqr_opts o = opts_or_default(op);
+    tsqr_status st = check_common<T>(m, n, A, lda, R, ldr, o);
+    if (st != TSQR_OK) return st;
+    if (o.panel > max_tsqr_n<T>()) return TSQR_ERR_UNSUPPORTED;
+    if (sizeof(T) == 4 && o.precision != TSQR_PRECISION_PLAIN) return TSQR_ERR_UNSUPPORTED;
+    return tsqr::qr_run<T>(m, n, A, lda, R, ldr, work, work_bytes, o, (cudaStream_t)stream);
+}
+
+// Reference-signature form: the caller's d_work (ldwork*n elements) is used
+// when it is large enough, the library's cached buffer otherwise.
+template <typename T, bool QR>
+tsqr_status ref_form(int m, int n, T* A, int lda, T* R, int ldr, T* d_work, int ldwork) {
+    tsqr_opts o = {};
+    if (m < 1 || n < 1) return TSQR_ERR_INVALID_ARG;
+    size_t need = QR ? tsqr::qr_workspace<T>(m, n, o) : tsqr::tsqr_plain_workspace<T>(m, n);
+    if (!QR && n > max_tsqr_n<T>()) return TSQR_ERR_UNSUPPORTED;
+    void* work = d_work;
+    size_t have = (d_work && ldwork > 0) ? (size_t)ldwork * (size_t)n * sizeof(T) : 0;
+    if (have < need) {
+        tsqr_status st;
+        work = tsqr::cached_workspace(need, &st);
+        if (!work) return st;
+        have = need;
+    }
+    return QR ? qr_ex<T>(m, n, A, lda, R, ldr, work, have, &o, nullptr)
+              : tsqr_ex<T>(m, n, A, lda, R, ldr, work, have, &o, nullptr);
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t tsqr_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opts* opts) {
+    (void)opts;
+    if (m < 1 || n < 1 || m < n) return 0;
+    if (elem_bytes == 4) return n <= 64 ? tsqr::tsqr_plain_workspace<float>(m, n) : 0;
+    if (elem_bytes == 8) return n <= 32 ? tsqr::tsqr_plain_workspace<double>(m, n) : 0;
+    return 0;
+}
+
+size_t qr_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opts* opts) {
+    const tsqr_opts o = opts_or_default(opts);
+    if (m < 1 || n < 1 || m < n) return 0;
+    if (elem_bytes == 4) return tsqr::qr_workspace<float>(m, n, o);
+    if (elem_bytes == 8) return tsqr::qr_workspace<double>(m, n, o);
+    return 0;
+}
+
+tsqr_status tsqr_s_ex(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
+                      size_t work_bytes, const tsqr_opts* opts, void* stream) {
+    return tsqr_ex<float>(m, n, A, lda, R, ldr, work, work_bytes, opts, stream);
+}
+tsqr_status tsqr_d_ex(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr, void* work,
+                      size_t work_bytes, const tsqr_opts* opts, void* stream) {
+    return tsqr_ex<double>(m, n, A, lda, R, ldr, work, work_bytes, opts, stream);
+}
+tsqr_status qr_s_ex(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
+                    size_t work_bytes, const tsqr_opts* opts, void* stream) {
+    return qr_ex<float>(m, n, A, lda, R, ldr, work, work_bytes, opts, stream);
+}
+tsqr_status qr_d_ex(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr, void* work,
+                    size_t work_bytes, const tsqr_opts* opts, void* stream) {
+    return qr_ex<double>(m, n, A, lda, R, ldr, work, work_bytes, opts, stream);
+}
+
+tsqr_status tsqr_float(int m, int n, float* A, int lda, float* R, int ldr, float* d_work, int ldwork) {
+    return ref_form<float, false>(m, n, A, lda, R, ldr, d_work, ldwork);
+}
+tsqr_status tsqr_double(int m, int n, double* A, int lda, double* R, int ldr, double* d_work, int ldwork) {
+    return ref_form<double, false>(m, n, A, lda, R, ldr, d_work, ldwork);
+}
+tsqr_status qr_float(int m, int n, float* A, int lda, float* R, int ldr, float* d_work, int ldwork) {
+    return ref_form<float, true>(m, n, A, lda, R, ldr, d_work, ldwork);
+}
+tsqr_status qr_double(int m, int n, double* A, int lda, double* R, int ldr, double* d_work, int ldwork) {
+    return ref_form<double, true>(m, n, A, lda, R, ldr, d_work, ldwork);
+}
+
+size_t tsqr_batched_workspace_bytes(int count, const int64_t* m, const int64_t* n) {
+    (void)count;
+    (void)m;
+    (void)n;
+    return 0;
+}
+
+tsqr_status tsqr_batched_s(int count, float* const* A, const int64_t* m, const int64_t* n, const int64_t* lda,
+                           float* const* R, const int64_t* ldr, void* work, size_t work_bytes,
+                           const tsqr_opts* opts, void* stream) {
+    (void)count; (void)A; (void)m; (void)n; (void)lda; (void)R; (void)ldr;
+    (void)work; (void)work_bytes; (void)opts; (void)stream;
+    return TSQR_ERR_UNSUPPORTED;
+}
+
+const char* tsqr_status_string(tsqr_status s) {
+    switch (s) {
+        case TSQR_OK: return "success";
+        case TSQR_ERR_INVALID_ARG: return "invalid argument (m, n, lda, ldr, pointer or options)";
+        case TSQR_ERR_UNSUPPORTED: return "size or option not supported";
+        case TSQR_ERR_WORKSPACE: return "workspace missing or too small";
+        case TSQR_ERR_CUDA: return "CUDA runtime error";
+        case TSQR_ERR_NO_DEVICE: return "no usable CUDA device";
+    }
+    return "unknown status";
+}
+
+const char* tsqr_version(void) { return "0.1.0"; }
+
+tsqr_status tsqr_profile(int kind, int elem_bytes, int64_t m, int64_t n, void* A, int64_t lda, void* R, int64_t ldr,
+                         void* work, size_t work_bytes, const tsqr_opts* opts, void* stream, float* launch_ms,
+                         int* launch_tag, int max_launch, int* n_launch) {
+    if (!launch_ms || !launch_tag || !n_launch || max_launch < 1) return TSQR_ERR_INVALID_ARG;
+    if (kind < 0 || kind > 1 || (elem_bytes != 4 && elem_bytes != 8)) return TSQR_ERR_INVALID_ARG;
+    tsqr::LaunchLog* log = new tsqr::LaunchLog();
+    const int nev = tsqr::LaunchLog::kMax + 1;
+    for (int i = 0; i < nev; ++i) cudaEventCreate(&log->ev[i]);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEventRecord(log->ev[0], s);
+    tsqr::tl_log = log;
+    tsqr_status st;
+    if (kind == 0)
+        st = elem_bytes == 4 ? tsqr_s_ex(m, n, (float*)A, lda, (float*)R, ldr, work, work_bytes, opts, stream)
+                             : tsqr_d_ex(m, n, (double*)A, lda, (double*)R, ldr, work, work_bytes, opts, stream);
+    else
+        st = elem_bytes == 4 ? qr_s_ex(m, n, (float*)A, lda, (float*)R, ldr, work, work_bytes, opts, stream)
+                             : qr_d_ex(m, n, (double*)A, lda, (double*)R, ldr, work, work_bytes, opts, stream);
+    tsqr::tl_log = nullptr;
+    int cnt = log->count;
+    if (st == TSQR_OK && cudaEventSynchronize(log->ev[cnt]) != cudaSuccess) st = TSQR_ERR_CUDA;
+    *n_launch = 0;
+    if (st == TSQR_OK) {
+        int k = cnt < max_launch ? cnt : max_launch;
+        for (int i = 0; i < k; ++i) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, log->ev[i], log->ev[i + 1]);
+            launch_ms[i] = ms;
+            launch_tag[i] = log->tag[i];
+        }
+        *n_launch = k;
+    }
+    for (int i = 0; i < nev; ++i) cudaEventDestroy(log->ev[i]);
+    delete log;
+    return st;
+}
+
+}  // extern "C"

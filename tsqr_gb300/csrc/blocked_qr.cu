@@ -1,0 +1,271 @@
+// blocked_qr.cu -- recursive blocked QR over TSQR panels (plain precision).
+//
+// Replaces qr<T> (block_QR.h:72-95): recursive block classical Gram-Schmidt,
+//   qr(A1);  R12 = A1^T A2;  A2 -= A1 R12;  qr(A2),
+// with TSQR on panels of width <= panel (32, the reference's N_B,
+// block_QR.h:5).  The reference's single naive kernel gemm_blockqr
+// (block_QR.h:7-60: one thread per output, a length-m dot with stride-lda
+// loads for op=T) becomes two tiled SIMT kernels:
+//   gemm_tn_partial + reduce_partials: R12 = A1^T A2, K = m split across
+//     CTAs into deterministic partial sums (no atomics), then summed;
+//   gemm_nn: A2 = A2 - A1 R12, streamed over row blocks.
+// Options the reference lacks: any split point (not only n/2 with
+// (n/2) % 32 == 0, block_QR.h:78-79), a second projection (CGS2) when
+// opts.reorth is set, and R21 written as zeros (the reference leaves it
+// unwritten).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace tsqr {
+
+namespace {
+
+constexpr int kTile = 64;  // output tile edge
+constexpr int kKt = 16;    // k step through shared memory
+
+// P_z (M x N, ld M) = sum over k in chunk z of A(k, i) * B(k, j);
+// A is K x M, B is K x N, both column-major.
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_tn_partial(int M, int N, int64_t K, const T* __restrict__ A,
+                                                       int64_t lda, const T* __restrict__ B, int64_t ldb,
+                                                       T* __restrict__ P, int64_t kchunk) {
+    __shared__ T As[kKt][kTile + 1];
+    __shared__ T Bs[kKt][kTile + 1];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int i0 = blockIdx.x * kTile, j0 = blockIdx.y * kTile;
+    const int64_t kbeg = (int64_t)blockIdx.z * kchunk;
+    const int64_t kend = min(K, kbeg + kchunk);
+    T acc[4][4] = {};
+    for (int64_t k0 = kbeg; k0 < kend; k0 += kKt) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int idx = tid + 256 * e;
+            const int kk = idx % kKt, col = idx / kKt;
+            const int64_t k = k0 + kk;
+            As[kk][col] = (k < kend && i0 + col < M) ? A[k + (int64_t)(i0 + col) * lda] : T(0);
+            Bs[kk][col] = (k < kend && j0 + col < N) ? B[k + (int64_t)(j0 + col) * ldb] : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kKt; ++kk) {
+            T a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                a[u] = As[kk][ty * 4 + u];
+                b[u] = Bs[kk][tx * 4 + u];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] += a[u] * b[v];
+        }
+        __syncthreads();
+    }
+    T* Pz = P + (int64_t)blockIdx.z * M * N;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int i = i0 + ty * 4 + u, j = j0 + tx * 4 + v;
+            if (i < M && j < N) Pz[i + (int64_t)j * M] = acc[u][v];
+        }
+}
+
+// C = alpha * sum_z P_z + beta * C  (C is M x N with ldc)
+template <typename T>
+__global__ void reduce_partials(int M, int N, int nz, const T* __restrict__ P, T alpha, T beta, T* C,
+                                int64_t ldc) {
+    const int64_t total = (int64_t)M * N;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        T s = 0;
+        for (int z = 0; z < nz; ++z) s += P[(int64_t)z * total + e];
+        const int i = (int)(e % M), j = (int)(e / M);
+        T* c = C + i + (int64_t)j * ldc;
+        *c = (beta == T(0)) ? alpha * s : alpha * s + beta * *c;
+    }
+}
+
+// C (M x N) = alpha * A (M x K) * B (K x N) + beta * C, column-major.
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_nn(int64_t M, int N, int K, T alpha, const T* __restrict__ A,
+                                               int64_t lda, const T* __restrict__ B, int64_t ldb, T beta, T* C,
+                                               int64_t ldc) {
+    __shared__ T As[kKt][kTile + 1];
+    __shared__ T Bs[kKt][kTile + 1];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int64_t i0 = (int64_t)blockIdx.x * kTile;
+    const int j0 = blockIdx.y * kTile;
+    T acc[4][4] = {};
+    for (int k0 = 0; k0 < K; k0 += kKt) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int idx = tid + 256 * e;
+            {  // A tile: kKt columns of 64 contiguous rows
+                const int row = idx % kTile, kk = idx / kTile;
+                const int k = k0 + kk;
+                As[kk][row] = (k < K && i0 + row < M) ? A[i0 + row + (int64_t)k * lda] : T(0);
+            }
+            {  // B tile: 64 columns of kKt contiguous k
+                const int kk = idx % kKt, col = idx / kKt;
+                const int k = k0 + kk;
+                Bs[kk][col] = (k < K && j0 + col < N) ? B[k + (int64_t)(j0 + col) * ldb] : T(0);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kKt; ++kk) {
+            T a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                a[u] = As[kk][ty + 16 * u];
+                b[u] = Bs[kk][tx * 4 + u];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] += a[u] * b[v];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int64_t i = i0 + ty + 16 * u;
+            const int j = j0 + tx * 4 + v;
+            if (i < M && j < N) {
+                T* c = C + i + (int64_t)j * ldc;
+                *c = alpha * acc[u][v] + beta * *c;
+            }
+        }
+}
+
+template <typename T>
+__global__ void axpy_block(int M, int N, const T* __restrict__ X, int64_t ldx, T* Y, int64_t ldy) {
+    const int64_t total = (int64_t)M * N;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % M), j = (int)(e / M);
+        Y[i + (int64_t)j * ldy] += X[i + (int64_t)j * ldx];
+    }
+}
+
+int panel_of(const tsqr_opts& o) { return o.panel > 0 ? o.panel : 32; }
+
+int64_t split_of(int64_t n, int nb) {
+    int64_t n1 = (n / 2) / nb * nb;
+    return std::max<int64_t>(n1, nb);
+}
+
+struct GemmPlan {
+    int nz;
+    int64_t kchunk;
+};
+
+GemmPlan tn_plan(int64_t M, int64_t N, int64_t K) {
+    const int64_t tiles = ceil_div(M, kTile) * ceil_div(N, kTile);
+    int64_t nz = std::max<int64_t>(1, ceil_div(2 * 152, tiles));
+    nz = std::min<int64_t>(nz, std::max<int64_t>(1, ceil_div(K, 256)));
+    int64_t kchunk = round_up(ceil_div(K, nz), kKt);
+    nz = ceil_div(K, kchunk);
+    return {(int)nz, kchunk};
+}
+
+// Workspace layout: [tsqr region | partial sums | reorth temp].
+struct QrWs {
+    size_t tsqr_bytes = 0, part_bytes = 0, tmp_bytes = 0;
+    size_t total() const { return tsqr_bytes + part_bytes + tmp_bytes; }
+};
+
+template <typename T>
+void qr_ws_walk(int64_t m, int64_t n, int nb, bool reorth, QrWs* w) {
+    if (n <= nb) {
+        w->tsqr_bytes = std::max(w->tsqr_bytes, (size_t)round_up((int64_t)tsqr_plain_workspace<T>(m, n), 256));
+        return;
+    }
+    const int64_t n1 = split_of(n, nb), n2 = n - n1;
+    GemmPlan gp = tn_plan(n1, n2, m);
+    w->part_bytes = std::max(w->part_bytes, (size_t)round_up((int64_t)gp.nz * n1 * n2 * (int64_t)sizeof(T), 256));
+    if (reorth) w->tmp_bytes = std::max(w->tmp_bytes, (size_t)round_up(n1 * n2 * (int64_t)sizeof(T), 256));
+    qr_ws_walk<T>(m, n1, nb, reorth, w);
+    qr_ws_walk<T>(m, n2, nb, reorth, w);
+}
+
+template <typename T>
+tsqr_status proj_tn(int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2, int64_t lda, T* P, T* C,
+                    int64_t ldc, T beta, cudaStream_t s) {
+    GemmPlan gp = tn_plan(n1, n2, m);
+    dim3 g((unsigned)ceil_div(n1, kTile), (unsigned)ceil_div(n2, kTile), (unsigned)gp.nz);
+    gemm_tn_partial<T><<<g, 256, 0, s>>>((int)n1, (int)n2, m, A1, lda, A2, lda, P, gp.kchunk);
+    log_launch(kTagGemmTN, s);
+    const int64_t total = n1 * n2;
+    int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 1024);
+    reduce_partials<T><<<blocks, 256, 0, s>>>((int)n1, (int)n2, gp.nz, P, T(1), beta, C, ldc);
+    log_launch(kTagReduce, s);
+    return TSQR_OK;
+}
+
+template <typename T>
+tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, char* ws, const QrWs& w,
+                   const tsqr_opts& o, cudaStream_t s) {
+    const int nb = panel_of(o);
+    if (n <= nb) return tsqr_plain<T>(m, n, A, lda, R, ldr, ws, w.tsqr_bytes, s);
+    const int64_t n1 = split_of(n, nb), n2 = n - n1;
+    T* A1 = A;
+    T* A2 = A + n1 * lda;
+    T* R11 = R;
+    T* R12 = R + n1 * ldr;
+    T* R22 = R + n1 * ldr + n1;
+    T* P = reinterpret_cast<T*>(ws + w.tsqr_bytes);
+    T* tmp = reinterpret_cast<T*>(ws + w.tsqr_bytes + w.part_bytes);
+    tsqr_status st = qr_rec<T>(m, n1, A1, lda, R11, ldr, ws, w, o, s);
+    if (st != TSQR_OK) return st;
+    proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), s);
+    dim3 g((unsigned)ceil_div(m, kTile), (unsigned)ceil_div(n2, kTile));
+    gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, R12, ldr, T(1), A2, lda);
+    log_launch(kTagGemmNN, s);
+    if (o.reorth) {
+        proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), s);
+        gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, tmp, n1, T(1), A2, lda);
+        log_launch(kTagGemmNN, s);
+        int blocks = (int)std::min<int64_t>(ceil_div(n1 * n2, 256), 1024);
+        axpy_block<T><<<blocks, 256, 0, s>>>((int)n1, (int)n2, tmp, n1, R12, ldr);
+        log_launch(kTagAxpy, s);
+    }
+    if (cudaMemset2DAsync(R + n1, ldr * sizeof(T), 0, n2 * sizeof(T), n1, s) != cudaSuccess) return TSQR_ERR_CUDA;
+    st = qr_rec<T>(m, n2, A2, lda, R22, ldr, ws, w, o, s);
+    if (st != TSQR_OK) return st;
+    return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
+}
+
+}  // namespace
+
+template <typename T>
+size_t qr_workspace(int64_t m, int64_t n, const tsqr_opts& o) {
+    QrWs w;
+    qr_ws_walk<T>(m, n, panel_of(o), o.reorth != 0, &w);
+    return w.total();
+}
+
+template <typename T>
+tsqr_status qr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
+                   const tsqr_opts& o, cudaStream_t s) {
+    QrWs w;
+    qr_ws_walk<T>(m, n, panel_of(o), o.reorth != 0, &w);
+    if (work == nullptr || work_bytes < w.total()) return TSQR_ERR_WORKSPACE;
+    return qr_rec<T>(m, n, A, lda, R, ldr, reinterpret_cast<char*>(work), w, o, s);
+}
+
+template size_t qr_workspace<float>(int64_t, int64_t, const tsqr_opts&);
+template size_t qr_workspace<double>(int64_t, int64_t, const tsqr_opts&);
+template tsqr_status qr_run<float>(int64_t, int64_t, float*, int64_t, float*, int64_t, void*, size_t,
+                                   const tsqr_opts&, cudaStream_t);
+template tsqr_status qr_run<double>(int64_t, int64_t, double*, int64_t, double*, int64_t, void*, size_t,
+                                    const tsqr_opts&, cudaStream_t);
+
+}  // namespace tsqr

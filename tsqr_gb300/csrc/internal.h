@@ -1,0 +1,48 @@
+// internal.h -- declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/tsqr_gb300.h"
+
+namespace tsqr {
+
+// Launch log for the instrumented entry point: when active on this host
+// thread, every kernel launch of the library records a CUDA event after it
+// on the launch stream, so per-launch device times can be read back.
+struct LaunchLog {
+    static constexpr int kMax = 512;
+    cudaEvent_t ev[kMax + 1];
+    int tag[kMax];
+    int count = 0;
+};
+extern thread_local LaunchLog* tl_log;
+inline void log_launch(int tag, cudaStream_t s) {
+    if (tl_log && tl_log->count < LaunchLog::kMax) {
+        tl_log->tag[tl_log->count] = tag;
+        cudaEventRecord(tl_log->ev[++tl_log->count], s);
+    }
+}
+// Launch tags: kind * 1000 + level.
+enum { kTagFactor = 1000, kTagApply = 2000, kTagGemmTN = 3000, kTagReduce = 4000, kTagGemmNN = 5000,
+       kTagAxpy = 6000, kTagTc = 7000, kTagBatched = 8000 };
+
+// Plain-precision TSQR tree (tsqr.cu).
+template <typename T>
+size_t tsqr_plain_workspace(int64_t m, int64_t n);
+template <typename T>
+tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
+                       cudaStream_t s);
+
+// Recursive blocked QR (blocked_qr.cu).
+template <typename T>
+size_t qr_workspace(int64_t m, int64_t n, const tsqr_opts& o);
+template <typename T>
+tsqr_status qr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
+                   const tsqr_opts& o, cudaStream_t s);
+
+// Library-owned per-device buffer for the reference-signature entry points.
+void* cached_workspace(size_t bytes, tsqr_status* st);
+
+}  // namespace tsqr

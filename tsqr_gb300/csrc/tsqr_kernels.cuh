@@ -1,0 +1,341 @@
+// tsqr_kernels.cuh -- CUDA-core (plain precision) TSQR tile kernels.
+//
+// A "level matrix" M (h x n, column-major, leading dimension ld) is cut into
+// tiles of B = NT*RPT rows.  Level 0 is the caller's A; level l+1 stacks the
+// n x n R factors of level l's tiles (h_{l+1} = tiles_l * n); the level with
+// a single tile is the root.  This is the reduction tree of the reference's
+// persistent tsqr_kernel (kernelQR.h:341-388) and of its two-level chunk
+// scheme (TallShinnyQR.h:106-127), restated as one tree with a tile height
+// chosen per (dtype, n) instead of the compile-time BLOCK_SIZE=128 and
+// NUM_SM=108 (kernelQR.h:3-4).
+//
+// factor_tiles: Householder QR of each tile (the reference's qr_kernel,
+//   kernelQR.h:69-220), LAPACK larfg form: H_j = I - tau_j v_j v_j^T with
+//   v_j(j) = 1 and R_jj = beta_j = -sign(alpha) ||x||, the same diagonal sign
+//   rule as kernelQR.h:139-142.  Instead of forming the tile's explicit Q in
+//   shared memory (kernelQR.h:224-290) it leaves the compact-WY form in place:
+//   the strict lower part of the tile holds V, the upper triangle of the
+//   tile's top n x n block holds T (H_0...H_{n-1} = I - V T V^T).  The tile
+//   lives in registers (RPT rows x NMAX columns per thread).  Each column
+//   costs two block barriers: one after the norm partials, one after the
+//   dot-product partials (the warp transpose-reduction of NMAX values, then a
+//   redundant per-warp finalisation instead of a third barrier).  The same
+//   reduction also yields column j of V^T V, from which T is formed once per
+//   tile: row i of T depends only on row i (T(i,j) = -tau_j sum_k T(i,k)
+//   S(k,j)), so thread i builds it alone.  R goes to the next level's rows
+//   [t*n, t*n+n), or to the caller's R at the root.  With NORM64 the norm,
+//   beta and tau are computed in FP64.
+//
+// apply_tiles: down-sweep (kernelQR.h:397-492 and tsgemm_tsqr,
+//   TallShinnyQR.h:11-74): given the parent's n x n block B_t (the root uses
+//   B = I), the tile's final Q is (I - V T V^T) [B_t; 0] = [B_t; 0] - V W,
+//   W = T (V_top^T B_t).  W needs only the tile's top block, so the bulk is a
+//   reduction-free (B x n)(n x n) product streamed as n rank-1 updates of
+//   each thread's rows; Q overwrites the tile in place.
+//
+// Rows of the last tile past the matrix end are treated as zero rows: they
+// never change, never enter a dot product and are never stored.
+#pragma once
+#include <type_traits>
+
+#include "common.cuh"
+
+namespace tsqr {
+
+template <typename T>
+struct FactorParams {
+    T* M;           // level matrix (tiles are factored in place)
+    int64_t ld;
+    int64_t h;      // rows of the level matrix
+    int n;
+    int64_t ntiles;
+    T* Rout;        // R of tile t goes to rows [t*n, t*n+n) of Rout
+    int64_t ldr;
+};
+
+template <typename T>
+struct ApplyParams {
+    T* M;
+    int64_t ld;
+    int64_t h;
+    int n;
+    int64_t ntiles;
+    const T* P;     // parent level's final Q (rows t*n.. of tile t); null = identity
+    int64_t ldp;
+};
+
+template <typename T, int NMAX, int NT, int RPT, int MINB, bool NORM64>
+__global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
+    constexpr int NW = NT / 32;
+    constexpr int B = NT * RPT;
+    static_assert(NT >= NMAX && NT % 32 == 0, "block too small");
+    using N64 = typename std::conditional<NORM64, double, T>::type;
+    __shared__ N64 s_part[NW];
+    __shared__ T s_alpha;
+    __shared__ T red[NW][NMAX];
+    __shared__ __align__(16) T wfin[NW][NMAX];
+    __shared__ T Ssh[NMAX][NMAX + 1];
+    __shared__ T Tsh[NMAX][NMAX + 1];
+    __shared__ T tau_sh[NMAX];
+    __shared__ T rdiag[NMAX];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n = p.n;
+
+    for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        const int64_t row0 = t * B;
+        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
+        T* tile = p.M + row0;
+
+        T x[RPT][NMAX];
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+            const int r = tid + NT * i;
+#pragma unroll
+            for (int c = 0; c < NMAX; ++c)
+                x[i][c] = (r < ht && c < n) ? tile[r + c * p.ld] : T(0);
+        }
+
+#pragma unroll
+        for (int j = 0; j < NMAX; ++j) {
+            if (j < n) {
+                // (a) sigma^2 = ||x(j+1:, j)||^2 and alpha = x(j, j)
+                N64 s = 0;
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) {
+                    const int r = tid + NT * i;
+                    if (r > j) s += (N64)x[i][j] * (N64)x[i][j];
+                    if (r == j) s_alpha = x[i][j];
+                }
+                s = warp_sum(s);
+                if (lane == 0) s_part[warp] = s;
+                __syncthreads();
+                N64 sigma2 = 0;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) sigma2 += s_part[w];
+                const N64 alpha = s_alpha;
+                N64 beta, tau, scale;
+                if (sigma2 == N64(0)) {
+                    tau = 0;
+                    beta = alpha;
+                    scale = 0;
+                } else {
+                    const N64 nrm = sqrt(alpha * alpha + sigma2);
+                    beta = (alpha >= N64(0)) ? -nrm : nrm;
+                    tau = (beta - alpha) / beta;
+                    scale = N64(1) / (alpha - beta);
+                }
+                const T taut = (T)tau;
+                const T scalet = (T)scale;
+                // (b) v_j below the diagonal (v_j(j) = 1 implicitly), and the
+                // partial dots: c > j: v^T x_c (trailing update); c < j:
+                // v_c^T v_j (column j of V^T V, for T)
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) {
+                    const int r = tid + NT * i;
+                    if (r > j) x[i][j] *= scalet;
+                }
+                T pc[NMAX];
+#pragma unroll
+                for (int c = 0; c < NMAX; ++c) pc[c] = 0;
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) {
+                    const int r = tid + NT * i;
+                    if (r >= j) {
+                        const T v = (r == j) ? T(1) : x[i][j];
+#pragma unroll
+                        for (int c = 0; c < NMAX; ++c)
+                            if (c != j) pc[c] += v * x[i][c];
+                    }
+                }
+                warp_reduce_to_smem<T, NMAX>(pc, red[warp], lane);
+                __syncthreads();
+                // (c) every warp sums the NW partials itself (no third barrier)
+                {
+                    constexpr int K = NMAX >= 32 ? NMAX / 32 : 1;
+#pragma unroll
+                    for (int kk = 0; kk < K; ++kk) {
+                        const int idx = (NMAX >= 32) ? lane * K + kk : lane;
+                        if (idx < NMAX) {
+                            T a = 0;
+#pragma unroll
+                            for (int w = 0; w < NW; ++w) a += red[w][idx];
+                            wfin[warp][idx] = a;
+                            if (warp == 0 && idx < j) Ssh[idx][j] = a;
+                        }
+                    }
+                    if (tid == 0) {
+                        tau_sh[j] = taut;
+                        rdiag[j] = (T)beta;
+                    }
+                }
+                __syncwarp();
+                // (d) trailing update x_c -= tau (v^T x_c) v over rows >= j
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) {
+                    const int r = tid + NT * i;
+                    if (r >= j) {
+                        const T tv = taut * ((r == j) ? T(1) : x[i][j]);
+#pragma unroll
+                        for (int c = j + 1; c < NMAX; ++c) x[i][c] -= tv * wfin[warp][c];
+                    }
+                }
+            }
+        }
+        __syncthreads();  // Ssh, tau_sh, rdiag complete
+
+        // T, one row per thread: T(i,i) = tau_i,
+        // T(i,j) = -tau_j sum_{k=i}^{j-1} T(i,k) S(k,j) for j > i.
+        if (tid < n) {
+            const int i = tid;
+            T trow[NMAX];
+#pragma unroll
+            for (int j = 0; j < NMAX; ++j) {
+                T val = T(0);
+                if (j == i) {
+                    val = tau_sh[j];
+                } else if (j > i && j < n) {
+                    T a = 0;
+#pragma unroll
+                    for (int k = 0; k < j; ++k)
+                        if (k >= i) a += trow[k] * Ssh[k][j];
+                    val = -tau_sh[j] * a;
+                }
+                trow[j] = val;
+            }
+#pragma unroll
+            for (int j = 0; j < NMAX; ++j) Tsh[i][j] = trow[j];
+        }
+        __syncthreads();
+
+        // R of this tile: row r < n is held by thread r (i = 0).
+        if (tid < n) {
+            const int r = tid;
+            T* Rt = p.Rout + t * n;
+#pragma unroll
+            for (int c = 0; c < NMAX; ++c) {
+                if (c < n) {
+                    T v = (c > r) ? x[0][c] : ((c == r) ? rdiag[r] : T(0));
+                    if (r >= ht) v = T(0);
+                    Rt[r + c * p.ldr] = v;
+                }
+            }
+        }
+        // V below the diagonal, T in the top block's upper triangle.
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+            const int r = tid + NT * i;
+            if (r < ht) {
+#pragma unroll
+                for (int c = 0; c < NMAX; ++c) {
+                    if (c < n) {
+                        const T v = (r > c) ? x[i][c] : Tsh[r][c];
+                        tile[r + c * p.ld] = v;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T, int NMAX>
+constexpr size_t apply_smem_bytes() {
+    return sizeof(T) * (size_t)NMAX * NMAX + 4 * sizeof(T) * (size_t)NMAX * (NMAX + 1);
+}
+
+template <typename T, int NMAX, int NT, int RPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) apply_tiles(ApplyParams<T> p) {
+    constexpr int B = NT * RPT;
+    // Ws: NMAX x NMAX, then Vt, Tt, Bs, Ys: NMAX x (NMAX+1) each, in dynamic
+    // shared memory (apply_smem_bytes), which can exceed 48 KB.
+    extern __shared__ __align__(16) unsigned char apply_smem[];
+    typedef T Row1[NMAX + 1];
+    typedef T Row0[NMAX];
+    Row0* Ws = reinterpret_cast<Row0*>(apply_smem);
+    Row1* Vt = reinterpret_cast<Row1*>(apply_smem + sizeof(T) * NMAX * NMAX);
+    Row1* Tt = Vt + NMAX;
+    Row1* Bs = Tt + NMAX;
+    Row1* Ys = Bs + NMAX;
+
+    const int tid = threadIdx.x;
+    const int n = p.n;
+
+    for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        const int64_t row0 = t * B;
+        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
+        T* tile = p.M + row0;
+
+        for (int idx = tid; idx < NMAX * NMAX; idx += NT) {
+            const int r = idx % NMAX, c = idx / NMAX;
+            const bool in = (r < ht && r < n && c < n);
+            const T v = in ? tile[r + c * p.ld] : T(0);
+            Vt[r][c] = (r > c) ? v : ((r == c && c < n) ? T(1) : T(0));
+            Tt[r][c] = (r <= c) ? v : T(0);
+            T b;
+            if (p.P)
+                b = (r < n && c < n) ? p.P[t * n + r + c * p.ldp] : T(0);
+            else
+                b = (r == c && r < n) ? T(1) : T(0);
+            Bs[r][c] = b;
+        }
+        __syncthreads();
+        // Y = V_top^T B
+        for (int idx = tid; idx < NMAX * NMAX; idx += NT) {
+            const int k = idx % NMAX, c = idx / NMAX;
+            T a = 0;
+            for (int r = k; r < NMAX; ++r) a += Vt[r][k] * Bs[r][c];
+            Ys[k][c] = a;
+        }
+        __syncthreads();
+        // W = T Y
+        for (int idx = tid; idx < NMAX * NMAX; idx += NT) {
+            const int k = idx % NMAX, c = idx / NMAX;
+            T a = 0;
+            for (int l = k; l < NMAX; ++l) a += Tt[k][l] * Ys[l][c];
+            Ws[k][c] = a;
+        }
+        __syncthreads();
+
+        // Q rows = [B; 0] - V W as n rank-1 updates of the thread's rows.
+        T q[RPT][NMAX];
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+            const int r = tid + NT * i;
+#pragma unroll
+            for (int c = 0; c < NMAX; ++c) q[i][c] = (r < n) ? Bs[r][c] : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < NMAX; ++k) {
+            if (k < n) {
+                T vk[RPT];
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) {
+                    const int r = tid + NT * i;
+                    // rows of the top block come masked from shared memory
+                    // (T above the diagonal, unit diagonal); the rest from
+                    // the tile
+                    vk[i] = (r < n) ? Vt[r][k] : ((r < ht) ? tile[r + k * p.ld] : T(0));
+                }
+#pragma unroll
+                for (int c = 0; c < NMAX; ++c) {
+                    const T w = Ws[k][c];
+#pragma unroll
+                    for (int i = 0; i < RPT; ++i) q[i][c] -= vk[i] * w;
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+            const int r = tid + NT * i;
+            if (r < ht) {
+#pragma unroll
+                for (int c = 0; c < NMAX; ++c)
+                    if (c < n) tile[r + c * p.ld] = q[i][c];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace tsqr
