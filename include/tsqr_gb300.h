@@ -92,6 +92,24 @@ tsqr_status tsqr_batched_s(int count, float* const* A, const int64_t* m, const i
                            const int64_t* lda, float* const* R, const int64_t* ldr,
                            void* work, size_t work_bytes, const tsqr_opts* opts, void* stream);
 
+/* FP32 TSQR that allocates nothing.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc: frameworks that have already
+ * reserved nearly all device memory for their own pool, programs with a
+ * memory budget set at start-up, callers that cannot afford the device-wide
+ * synchronisation a cudaFree may cause, and callers of the reference's
+ * interface whose d_work cannot grow.  Same arithmetic and results as
+ * tsqr_s_ex with PLAIN precision; the tree workspace lives in one static
+ * device array of TSQR_NOALLOC_SCRATCH_BYTES inside the library, held by
+ * every GPU that loads the library until exit.  Problems whose workspace
+ * (tsqr_workspace_bytes) exceeds that size return TSQR_ERR_WORKSPACE
+ * without launching (with n = 32, up to about 1.9 million rows fit).
+ * The first call on a device looks up the array's device address with that
+ * device current; make it before any stream capture.  All calls on a
+ * device share the array: calls that overlap on the GPU race, so the caller
+ * must order them (one stream, or explicit synchronisation). */
+#define TSQR_NOALLOC_SCRATCH_BYTES (16u << 20)
+tsqr_status tsqr_s_noalloc(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* stream);
+
 /* Instrumentation (no counterpart in the reference): runs tsqr (kind 0) or
  * qr (kind 1) exactly as the _ex entry points do, recording a CUDA event on
  * `stream` before the first and after every kernel launch; synchronizes on

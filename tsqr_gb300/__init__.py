@@ -62,6 +62,7 @@ EXPORTS = {
     "tsqr_batched_workspace_bytes": ([ctypes.c_int, _p, _p], ctypes.c_size_t),
     "tsqr_batched_s": ([ctypes.c_int, _p, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p],
                        ctypes.c_int),
+    "tsqr_s_noalloc": ([_i64, _i64, _p, _i64, _p, _i64, _p], ctypes.c_int),
     "tsqr_profile": ([ctypes.c_int, ctypes.c_int, _i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t,
                       ctypes.POINTER(Opts), _p, _p, _p, ctypes.c_int, _p], ctypes.c_int),
     "tsqr_status_string": ([ctypes.c_int], ctypes.c_char_p),
