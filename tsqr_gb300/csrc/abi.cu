@@ -43,6 +43,9 @@ tsqr_status tsqr_ex(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, 
     if (n > max_tsqr_n<T>()) return TSQR_ERR_UNSUPPORTED;
     if (sizeof(T) == 8 || o.precision == TSQR_PRECISION_PLAIN)
         return tsqr::tsqr_plain<T>(m, n, A, lda, R, ldr, work, work_bytes, (cudaStream_t)stream);
+    if (o.precision == TSQR_PRECISION_TF32X3)
+        return tsqr::tsqr_precision(m, n, reinterpret_cast<float*>(A), lda, reinterpret_cast<float*>(R), ldr, work,
+                                    work_bytes, (cudaStream_t)stream);
     return TSQR_ERR_UNSUPPORTED;
 }
 
@@ -82,8 +85,10 @@ tsqr_status ref_form(int m, int n, T* A, int lda, T* R, int ldr, T* d_work, int 
 extern "C" {
 
 size_t tsqr_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opts* opts) {
-    (void)opts;
+    const tsqr_opts o = opts_or_default(opts);
     if (m < 1 || n < 1 || m < n) return 0;
+    if (elem_bytes == 4 && o.precision == TSQR_PRECISION_TF32X3)
+        return n <= 64 ? tsqr::tsqr_precision_workspace(m, n) : 0;
     if (elem_bytes == 4) return n <= 64 ? tsqr::tsqr_plain_workspace<float>(m, n) : 0;
     if (elem_bytes == 8) return n <= 32 ? tsqr::tsqr_plain_workspace<double>(m, n) : 0;
     return 0;

@@ -46,3 +46,10 @@ tsqr_status qr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, v
 void* cached_workspace(size_t bytes, tsqr_status* st);
 
 }  // namespace tsqr
+
+namespace tsqr {
+// Precision form of TSQR (tsqr.cu + tc_apply.cu), FP32 only.
+size_t tsqr_precision_workspace(int64_t m, int64_t n);
+tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
+                           size_t work_bytes, cudaStream_t s);
+}  // namespace tsqr

@@ -1,0 +1,228 @@
+// tc_apply.cu -- Q assembly of the TSQR down-sweep on the tcgen05 tensor
+// cores (precision form, FP32 entry points).
+//
+// Same arithmetic as apply_tiles (the down-sweep of kernelQR.h:397-492 and
+// tsgemm_tsqr, TallShinnyQR.h:11-74): for each tile, Q = [B;0] - V W with
+// W = T (V_top^T B).  The small n x n products that give W stay on CUDA
+// cores in FP32.  The bulk product V W (tile rows x n x n) runs as
+// tcgen05.mma kind::tf32 with FP32 accumulation in TMEM, with both operands
+// split into TF32 hi + lo parts and three products hi*hi + hi*lo + lo*hi, so
+// the result carries close to FP32 accuracy (about 2^-21 relative per
+// product).
+//
+// One CTA of 128 threads (one warpgroup) takes a tile and walks it in blocks
+// of 128 rows: each thread loads its row of V (coalesced column loads),
+// splits it and stores both halves as the K-major A operand; one thread
+// issues 3 * NMAX/8 MMAs (M = 128, N = NMAX, K = 8) and commits them to an
+// mbarrier; each warp then reads its 32 TMEM lanes (its 32 rows) and writes
+// Q.  The next block's row is loaded into registers before the wait, so the
+// global loads overlap the tensor-core work.
+#include <cuda_runtime.h>
+
+#include "internal.h"
+#include "tc.cuh"
+#include "tsqr_kernels.cuh"
+
+namespace tsqr {
+
+namespace {
+
+template <int NMAX>
+struct TcApplySmem {
+    uint32_t a_hi[128 * NMAX];     // K-major A operand, one 128-row block
+    uint32_t a_lo[128 * NMAX];
+    uint32_t b_hi[NMAX * NMAX];    // K-major B operand: W (K = NMAX rows of W, N = NMAX)
+    uint32_t b_lo[NMAX * NMAX];
+    float Ws[NMAX][NMAX];
+    float Vt[NMAX][NMAX + 1];
+    float Tt[NMAX][NMAX + 1];
+    float Bs[NMAX][NMAX + 1];
+    float Ys[NMAX][NMAX + 1];
+    unsigned long long mbar;
+    uint32_t tmem_slot;
+};
+
+template <int NMAX, int B>
+__global__ void __launch_bounds__(128) tc_apply_tiles(ApplyParams<float> p, int* err) {
+    static_assert(NMAX % 16 == 0 && NMAX <= 256 && B % 128 == 0, "bad shape");
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    TcApplySmem<NMAX>& S = *reinterpret_cast<TcApplySmem<NMAX>*>(tc_smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int n = p.n;
+    constexpr uint32_t kCols = NMAX < 32 ? 32 : NMAX;  // TMEM columns: power of 2 >= 32
+    constexpr uint32_t idesc = tc::idesc_tf32(128, NMAX);
+    constexpr uint32_t SBO = NMAX * 32;  // bytes between 8-row groups of a K-major tile with K = NMAX
+
+    const uint32_t mbar = tc::smem_u32(&S.mbar);
+    if (warp == 0) tc::tmem_alloc(&S.tmem_slot, kCols);
+    if (tid == 0) {
+        tc::mbar_init(mbar, 1);
+        tc::fence_mbar_init();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = S.tmem_slot;
+    uint32_t phase = 0;
+    bool ok = true;
+
+    for (int64_t t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
+        const int64_t row0 = t * B;
+        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
+        float* tile = p.M + row0;
+
+        // --- W = T (V_top^T B) on CUDA cores, then W as the B operand -----
+        for (int idx = tid; idx < NMAX * NMAX; idx += 128) {
+            const int r = idx % NMAX, c = idx / NMAX;
+            const bool in = (r < ht && r < n && c < n);
+            const float v = in ? tile[r + c * p.ld] : 0.f;
+            S.Vt[r][c] = (r > c) ? v : ((r == c && c < n) ? 1.f : 0.f);
+            S.Tt[r][c] = (r <= c) ? v : 0.f;
+            float b;
+            if (p.P)
+                b = (r < n && c < n) ? p.P[t * n + r + c * p.ldp] : 0.f;
+            else
+                b = (r == c && r < n) ? 1.f : 0.f;
+            S.Bs[r][c] = b;
+        }
+        __syncthreads();
+        for (int idx = tid; idx < NMAX * NMAX; idx += 128) {
+            const int k = idx % NMAX, c = idx / NMAX;
+            float a = 0;
+#pragma unroll
+            for (int r = 0; r < NMAX; ++r) a += S.Vt[r][k] * S.Bs[r][c];
+            S.Ys[k][c] = a;
+        }
+        __syncthreads();
+        for (int idx = tid; idx < NMAX * NMAX; idx += 128) {
+            const int k = idx % NMAX, c = idx / NMAX;
+            float a = 0;
+#pragma unroll
+            for (int l = 0; l < NMAX; ++l) a += S.Tt[k][l] * S.Ys[l][c];
+            S.Ws[k][c] = a;
+            // B operand element (row = output column c, K index k)
+            uint32_t hi, lo;
+            tc::split_tf32(a, hi, lo);
+            const uint32_t off = tc::kmajor_off(c, k, NMAX) >> 2;
+            S.b_hi[off] = hi;
+            S.b_lo[off] = lo;
+        }
+
+        // --- blocks of 128 rows ------------------------------------------
+        float vnext[NMAX];
+        auto load_row = [&](int blk, float (&v)[NMAX]) {
+            const int r = blk * 128 + tid;
+#pragma unroll
+            for (int k = 0; k < NMAX; ++k) {
+                float x;
+                if (r < n)
+                    x = 0.f;  // top-block rows come masked from Vt below
+                else
+                    x = (r < ht && k < n) ? tile[r + (int64_t)k * p.ld] : 0.f;
+                v[k] = x;
+            }
+        };
+        const int nblk = (ht + 127) / 128;
+        load_row(0, vnext);
+        __syncthreads();  // Vt complete (masked top rows)
+        for (int blk = 0; blk < nblk; ++blk) {
+            const int r = blk * 128 + tid;
+            float v[NMAX];
+#pragma unroll
+            for (int k = 0; k < NMAX; ++k) v[k] = (r < n) ? S.Vt[r][k] : vnext[k];
+#pragma unroll
+            for (int k4 = 0; k4 < NMAX; k4 += 4) {
+                uint4 hi, lo;
+                tc::split_tf32(v[k4 + 0], hi.x, lo.x);
+                tc::split_tf32(v[k4 + 1], hi.y, lo.y);
+                tc::split_tf32(v[k4 + 2], hi.z, lo.z);
+                tc::split_tf32(v[k4 + 3], hi.w, lo.w);
+                const uint32_t off = tc::kmajor_off(tid, k4, NMAX);
+                *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(S.a_hi) + off) = hi;
+                *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(S.a_lo) + off) = lo;
+            }
+            tc::fence_smem_to_async();
+            tc::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                const uint32_t ah = tc::smem_u32(S.a_hi), al = tc::smem_u32(S.a_lo);
+                const uint32_t bh = tc::smem_u32(S.b_hi), bl = tc::smem_u32(S.b_lo);
+#pragma unroll
+                for (int ks = 0; ks < NMAX / 8; ++ks) {
+                    const uint32_t ko = ks * 256;  // two core matrices of 16 bytes of K
+                    const uint64_t dah = tc::smem_desc(ah + ko, 128, SBO), dal = tc::smem_desc(al + ko, 128, SBO);
+                    const uint64_t dbh = tc::smem_desc(bh + ko, 128, SBO), dbl = tc::smem_desc(bl + ko, 128, SBO);
+                    tc::mma_tf32(tmem, dah, dbh, idesc, ks > 0);
+                    tc::mma_tf32(tmem, dah, dbl, idesc, true);
+                    tc::mma_tf32(tmem, dal, dbh, idesc, true);
+                }
+                tc::mma_commit(mbar);
+            }
+            // prefetch the next block's rows while the tensor core works
+            if (blk + 1 < nblk) load_row(blk + 1, vnext);
+            const bool waited = tc::mbar_wait(mbar, phase);
+            // a timed-out wait anywhere stops the whole CTA (uniform decision)
+            if (__syncthreads_or(!waited)) {
+                ok = false;
+                if (tid == 0) atomicExch(err, 1);
+                break;
+            }
+            phase ^= 1u;
+            tc::fence_after_sync();
+            // epilogue: warp w owns TMEM lanes 32w..32w+31 = rows of the block
+            float d[NMAX];
+#pragma unroll
+            for (int c8 = 0; c8 < NMAX; c8 += 8) {
+                float d8[8];
+                tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c8, d8);
+#pragma unroll
+                for (int e = 0; e < 8; ++e) d[c8 + e] = d8[e];
+            }
+            tc::tmem_ld_wait();
+            if (r < ht) {
+#pragma unroll
+                for (int c = 0; c < NMAX; ++c)
+                    if (c < n) tile[r + (int64_t)c * p.ld] = ((r < n) ? S.Bs[r][c] : 0.f) - d[c];
+            }
+            tc::fence_before_sync();
+            __syncthreads();  // TMEM and the A buffers are free for the next block
+        }
+    }
+    if (!ok) {
+        // give the MMAs still in flight a bounded chance to retire before
+        // the TMEM they write is released
+        (void)tc::mbar_wait(mbar, phase);
+    }
+    tc::fence_after_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, kCols);
+}
+
+template <int NMAX, int B>
+void launch(const ApplyParams<float>& p, int grid, int* err, cudaStream_t s) {
+    constexpr size_t smem = sizeof(TcApplySmem<NMAX>) + 1024;
+    static bool attr = [] {
+        return cudaFuncSetAttribute(tc_apply_tiles<NMAX, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem) == cudaSuccess;
+    }();
+    (void)attr;
+    tc_apply_tiles<NMAX, B><<<grid, 128, smem, s>>>(p, err);
+}
+
+}  // namespace
+
+// Tile heights must match the factor configuration of the precision path.
+bool tc_apply_level(const ApplyParams<float>& p, int nmax, int rows, int* err, cudaStream_t s) {
+    const int grid = (int)(p.ntiles < 1 ? 1 : (p.ntiles > (1 << 30) ? (1 << 30) : p.ntiles));
+    if (nmax == 32 && rows == 512) {
+        launch<32, 512>(p, grid, err, s);
+    } else if (nmax == 64 && rows == 256) {
+        launch<64, 256>(p, grid, err, s);
+    } else {
+        return false;
+    }
+    return true;
+}
+
+}  // namespace tsqr

@@ -23,20 +23,22 @@ thread_local LaunchLog* tl_log = nullptr;
 
 namespace {
 
-template <typename T, int NMAX, int NT, int RPT, int MINB, int AMINB, bool NORM64 = false>
+template <typename T, int NMAX, int NT, int RPT, int MINB, int AMINB, int ANT = NT, bool NORM64 = false>
 struct TileCfg {
+    static_assert((NT * RPT) % ANT == 0, "apply block must divide the tile");
+    static constexpr int ARPT = NT * RPT / ANT;
     static constexpr int kRows = NT * RPT;
     static void factor(const FactorParams<T>& p, int grid, cudaStream_t s) {
         factor_tiles<T, NMAX, NT, RPT, MINB, NORM64><<<grid, NT, 0, s>>>(p);
     }
     static void apply(const ApplyParams<T>& p, int grid, cudaStream_t s) {
-        constexpr size_t smem = apply_smem_bytes<T, NMAX>();
+        constexpr size_t smem = apply_smem_bytes<T, NMAX, ANT * ARPT>();
         static bool attr = [] {
-            return cudaFuncSetAttribute(apply_tiles<T, NMAX, NT, RPT, AMINB>,
+            return cudaFuncSetAttribute(apply_tiles<T, NMAX, ANT, ARPT, AMINB>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
         }();
         (void)attr;
-        apply_tiles<T, NMAX, NT, RPT, AMINB><<<grid, NT, smem, s>>>(p);
+        apply_tiles<T, NMAX, ANT, ARPT, AMINB><<<grid, ANT, smem, s>>>(p);
     }
 };
 
@@ -62,14 +64,14 @@ KernelSet<T> make_set() {
 KernelSet<float> pick(float*, int n) {
     if (n <= 8) return make_set<TileCfg<float, 8, 256, 4, 3, 3>, float>();
     if (n <= 16) return make_set<TileCfg<float, 16, 256, 2, 2, 3>, float>();
-    if (n <= 32) return make_set<TileCfg<float, 32, 256, 2, 2, 1>, float>();
+    if (n <= 32) return make_set<TileCfg<float, 32, 128, 4, 2, 2, 256>, float>();
     if (n <= 64) return make_set<TileCfg<float, 64, 256, 1, 1, 1>, float>();
     return KernelSet<float>();
 }
 KernelSet<double> pick(double*, int n) {
     if (n <= 8) return make_set<TileCfg<double, 8, 256, 2, 2, 3>, double>();
     if (n <= 16) return make_set<TileCfg<double, 16, 256, 2, 1, 2>, double>();
-    if (n <= 32) return make_set<TileCfg<double, 32, 256, 1, 1, 1>, double>();
+    if (n <= 32) return make_set<TileCfg<double, 32, 256, 1, 1, 2>, double>();
     return KernelSet<double>();
 }
 
@@ -148,8 +150,142 @@ tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ld
         ap.ntiles = lv[l].ntiles;
         ap.P = (l == L - 1) ? nullptr : lv[l + 1].M;
         ap.ldp = (l == L - 1) ? 0 : lv[l + 1].ld;
+        constexpr int ve = 16 / sizeof(T);
+        ap.vec = (lv[l].ld % ve == 0 && (reinterpret_cast<uintptr_t>(lv[l].M) % 16) == 0) ? 1 : 0;
         ks.apply(ap, (int)std::min<int64_t>(lv[l].ntiles, 1 << 30), s);
         log_launch(kTagApply + l, s);
+    }
+    return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------------------
+// Precision form (FP32 entry points): the tile factorisation stays FP32 on
+// CUDA cores with the per-column norm, beta and tau in FP64; the root of the
+// tree (the stacked R factors of the last level, at most one tile) is
+// factored in FP64 by the double-precision tree and converted back; every
+// Q assembly of the down-sweep runs on tcgen05 in TF32x3 (tc_apply.cu).
+// Workspace: [status word (256 B) | level matrices | FP64 root copy | FP64
+// root-tree workspace].
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename A, typename B>
+__global__ void convert_matrix(int64_t h, int n, const A* __restrict__ src, int64_t lds, B* __restrict__ dst,
+                               int64_t ldd) {
+    const int64_t total = h * n;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e % h, c = e / h;
+        dst[r + c * ldd] = (B)src[r + c * lds];
+    }
+}
+
+template <typename A, typename B>
+void convert(int64_t h, int n, const A* src, int64_t lds, B* dst, int64_t ldd, cudaStream_t s) {
+    const int64_t total = h * n;
+    const int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 1024);
+    convert_matrix<A, B><<<blocks, 256, 0, s>>>(h, n, src, lds, dst, ldd);
+}
+
+struct PrecCfg {
+    int nmax = 0, rows = 0;
+    KernelSet<float> ks;
+};
+
+PrecCfg pick_precision(int n) {
+    PrecCfg c;
+    if (n <= 32) {
+        c.nmax = 32;
+        c.ks = make_set<TileCfg<float, 32, 128, 4, 2, 2, 256, true>, float>();
+    } else if (n <= 64) {
+        c.nmax = 64;
+        c.ks = make_set<TileCfg<float, 64, 256, 1, 1, 1, 256, true>, float>();
+    }
+    c.rows = c.ks.rows;
+    return c;
+}
+
+struct PrecLayout {
+    size_t status = 0, levels = 0, root = 0, rootws = 0, total = 0;
+};
+
+PrecLayout prec_layout(int64_t m, int64_t n, const PrecCfg& c) {
+    PrecLayout L;
+    L.status = 0;
+    L.levels = kAlign;
+    std::vector<Level<float>> lv;
+    const size_t lev = plan_levels<float>(m, n, nullptr, m, c.rows, nullptr, &lv);
+    L.root = L.levels + lev;
+    const int64_t hroot = lv.back().h;
+    const bool root64 = n <= 32;
+    const size_t rootbytes = root64 ? (size_t)round_up(hroot * n * 8 + n * n * 8, (int64_t)kAlign) : 0;
+    L.rootws = L.root + rootbytes;
+    L.total = L.rootws + (root64 ? round_up((int64_t)tsqr_plain_workspace<double>(hroot, n), (int64_t)kAlign) : 0);
+    return L;
+}
+
+}  // namespace
+
+bool tc_apply_level(const ApplyParams<float>& p, int nmax, int rows, int* err, cudaStream_t s);
+
+size_t tsqr_precision_workspace(int64_t m, int64_t n) {
+    PrecCfg c = pick_precision((int)n);
+    if (!c.ks.factor) return 0;
+    return prec_layout(m, n, c).total;
+}
+
+tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
+                           size_t work_bytes, cudaStream_t s) {
+    PrecCfg c = pick_precision((int)n);
+    if (!c.ks.factor) return TSQR_ERR_UNSUPPORTED;
+    const PrecLayout PL = prec_layout(m, n, c);
+    if (work == nullptr || work_bytes < PL.total) return TSQR_ERR_WORKSPACE;
+    char* base = reinterpret_cast<char*>(work);
+    int* err = reinterpret_cast<int*>(base + PL.status);
+    std::vector<Level<float>> lv;
+    plan_levels<float>(m, n, A, lda, c.rows, base + PL.levels, &lv);
+    const int L = (int)lv.size();
+    if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
+    const bool root64 = n <= 32;
+    const int top = root64 ? L - 1 : L;  // levels factored in FP32 below the root
+    for (int l = 0; l < top; ++l) {
+        FactorParams<float> fp;
+        fp.M = lv[l].M;
+        fp.ld = lv[l].ld;
+        fp.h = lv[l].h;
+        fp.n = (int)n;
+        fp.ntiles = lv[l].ntiles;
+        fp.Rout = (l == L - 1) ? R : lv[l + 1].M;
+        fp.ldr = (l == L - 1) ? ldr : lv[l + 1].ld;
+        c.ks.factor(fp, (int)std::min<int64_t>(lv[l].ntiles, 1 << 30), s);
+        log_launch(kTagFactor + l, s);
+    }
+    if (root64) {
+        // FP64 root combine: the last level (at most one tile of stacked R
+        // factors, or A itself when m fits one tile) factored in double.
+        const Level<float>& rt = lv[L - 1];
+        double* Qd = reinterpret_cast<double*>(base + PL.root);
+        double* Rd = Qd + rt.h * n;
+        convert<float, double>(rt.h, (int)n, rt.M, rt.ld, Qd, rt.h, s);
+        log_launch(kTagTc + 900, s);
+        tsqr_status st = tsqr_plain<double>(rt.h, n, Qd, rt.h, Rd, n, base + PL.rootws, PL.total - PL.rootws, s);
+        if (st != TSQR_OK) return st;
+        convert<double, float>(rt.h, (int)n, Qd, rt.h, rt.M, rt.ld, s);
+        convert<double, float>(n, (int)n, Rd, n, R, ldr, s);
+        log_launch(kTagTc + 901, s);
+    }
+    for (int l = (root64 ? L - 2 : L - 1); l >= 0; --l) {
+        ApplyParams<float> ap;
+        ap.M = lv[l].M;
+        ap.ld = lv[l].ld;
+        ap.h = lv[l].h;
+        ap.n = (int)n;
+        ap.ntiles = lv[l].ntiles;
+        ap.P = (l == L - 1) ? nullptr : lv[l + 1].M;
+        ap.ldp = (l == L - 1) ? 0 : lv[l + 1].ld;
+        ap.vec = 0;
+        if (!tc_apply_level(ap, c.nmax, c.rows, err, s)) return TSQR_ERR_UNSUPPORTED;
+        log_launch(kTagTc + l, s);
     }
     return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
 }

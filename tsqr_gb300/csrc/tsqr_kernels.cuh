@@ -62,13 +62,15 @@ struct ApplyParams {
     int64_t ntiles;
     const T* P;     // parent level's final Q (rows t*n.. of tile t); null = identity
     int64_t ldp;
+    int vec;        // 1: ld and the level base allow 16-byte copies
 };
 
 template <typename T, int NMAX, int NT, int RPT, int MINB, bool NORM64>
 __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
     constexpr int NW = NT / 32;
     constexpr int B = NT * RPT;
-    static_assert(NT >= NMAX && NT % 32 == 0, "block too small");
+    constexpr int U = 4;  // columns per unrolled group
+    static_assert(NT >= NMAX && NT % 32 == 0 && NMAX % U == 0, "bad tile configuration");
     using N64 = typename std::conditional<NORM64, double, T>::type;
     __shared__ N64 s_part[NW];
     __shared__ T s_alpha;
@@ -81,105 +83,135 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int n = p.n;
+    const int G = (n + U - 1) / U;
+    const int shift = (U * G) % NMAX;  // register position c ends up holding column (c + shift) % NMAX
 
     for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
         const int64_t row0 = t * B;
         const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
         T* tile = p.M + row0;
 
-        T x[RPT][NMAX];
+        // y[i][c]: row tid + NT*i.  The column loop runs in groups of U
+        // columns; after each group the register row rotates left by U, so at
+        // group g position c < n - U*g holds column U*g + c (positions 0..U-1
+        // are the group's columns) and position NMAX - U*g + k holds the
+        // finished reflector v_k.  All register indices stay compile-time
+        // while the code holds U column steps instead of NMAX.
+        T y[RPT][NMAX];
 #pragma unroll
         for (int i = 0; i < RPT; ++i) {
             const int r = tid + NT * i;
 #pragma unroll
             for (int c = 0; c < NMAX; ++c)
-                x[i][c] = (r < ht && c < n) ? tile[r + c * p.ld] : T(0);
+                y[i][c] = (r < ht && c < n) ? tile[r + c * p.ld] : T(0);
         }
 
+#pragma unroll 1
+        for (int g = 0; g < G; ++g) {
+            const int base = U * g;
+            const int live = n - base;      // positions [0, live): columns base .. n-1
+            const int past0 = NMAX - base;  // positions [past0, NMAX): v_0 .. v_{base-1}
 #pragma unroll
-        for (int j = 0; j < NMAX; ++j) {
-            if (j < n) {
-                // (a) sigma^2 = ||x(j+1:, j)||^2 and alpha = x(j, j)
-                N64 s = 0;
+            for (int u = 0; u < U; ++u) {
+                const int j = base + u;
+                if (j < n) {
+                    // (a) sigma^2 = ||x(j+1:, j)||^2 and alpha = x(j, j)
+                    N64 s = 0;
 #pragma unroll
-                for (int i = 0; i < RPT; ++i) {
-                    const int r = tid + NT * i;
-                    if (r > j) s += (N64)x[i][j] * (N64)x[i][j];
-                    if (r == j) s_alpha = x[i][j];
-                }
-                s = warp_sum(s);
-                if (lane == 0) s_part[warp] = s;
-                __syncthreads();
-                N64 sigma2 = 0;
-#pragma unroll
-                for (int w = 0; w < NW; ++w) sigma2 += s_part[w];
-                const N64 alpha = s_alpha;
-                N64 beta, tau, scale;
-                if (sigma2 == N64(0)) {
-                    tau = 0;
-                    beta = alpha;
-                    scale = 0;
-                } else {
-                    const N64 nrm = sqrt(alpha * alpha + sigma2);
-                    beta = (alpha >= N64(0)) ? -nrm : nrm;
-                    tau = (beta - alpha) / beta;
-                    scale = N64(1) / (alpha - beta);
-                }
-                const T taut = (T)tau;
-                const T scalet = (T)scale;
-                // (b) v_j below the diagonal (v_j(j) = 1 implicitly), and the
-                // partial dots: c > j: v^T x_c (trailing update); c < j:
-                // v_c^T v_j (column j of V^T V, for T)
-#pragma unroll
-                for (int i = 0; i < RPT; ++i) {
-                    const int r = tid + NT * i;
-                    if (r > j) x[i][j] *= scalet;
-                }
-                T pc[NMAX];
-#pragma unroll
-                for (int c = 0; c < NMAX; ++c) pc[c] = 0;
-#pragma unroll
-                for (int i = 0; i < RPT; ++i) {
-                    const int r = tid + NT * i;
-                    if (r >= j) {
-                        const T v = (r == j) ? T(1) : x[i][j];
-#pragma unroll
-                        for (int c = 0; c < NMAX; ++c)
-                            if (c != j) pc[c] += v * x[i][c];
+                    for (int i = 0; i < RPT; ++i) {
+                        const int r = tid + NT * i;
+                        if (r > j) s += (N64)y[i][u] * (N64)y[i][u];
+                        if (r == j) s_alpha = y[i][u];
                     }
-                }
-                warp_reduce_to_smem<T, NMAX>(pc, red[warp], lane);
-                __syncthreads();
-                // (c) every warp sums the NW partials itself (no third barrier)
-                {
-                    constexpr int K = NMAX >= 32 ? NMAX / 32 : 1;
+                    s = warp_sum(s);
+                    if (lane == 0) s_part[warp] = s;
+                    __syncthreads();
+                    N64 sigma2 = 0;
 #pragma unroll
-                    for (int kk = 0; kk < K; ++kk) {
-                        const int idx = (NMAX >= 32) ? lane * K + kk : lane;
-                        if (idx < NMAX) {
-                            T a = 0;
+                    for (int w = 0; w < NW; ++w) sigma2 += s_part[w];
+                    const N64 alpha = s_alpha;
+                    N64 beta, tau, scale;
+                    if (sigma2 == N64(0)) {
+                        tau = 0;
+                        beta = alpha;
+                        scale = 0;
+                    } else {
+                        const N64 nrm = sqrt(alpha * alpha + sigma2);
+                        beta = (alpha >= N64(0)) ? -nrm : nrm;
+                        tau = (beta - alpha) / beta;
+                        scale = N64(1) / (alpha - beta);
+                    }
+                    const T taut = (T)tau;
+                    const T scalet = (T)scale;
+                    // (b) v_j below the diagonal (v_j(j) = 1 implicitly), then
+                    // v_j . y[c] for every other position: trailing columns
+                    // (update) and finished reflectors (column j of V^T V)
 #pragma unroll
-                            for (int w = 0; w < NW; ++w) a += red[w][idx];
-                            wfin[warp][idx] = a;
-                            if (warp == 0 && idx < j) Ssh[idx][j] = a;
+                    for (int i = 0; i < RPT; ++i) {
+                        const int r = tid + NT * i;
+                        if (r > j) y[i][u] *= scalet;
+                    }
+                    T pc[NMAX];
+#pragma unroll
+                    for (int c = 0; c < NMAX; ++c) pc[c] = 0;
+#pragma unroll
+                    for (int i = 0; i < RPT; ++i) {
+                        const int r = tid + NT * i;
+                        if (r >= j) {
+                            const T v = (r == j) ? T(1) : y[i][u];
+#pragma unroll
+                            for (int c = 0; c < NMAX; ++c)
+                                if (c != u) pc[c] += v * y[i][c];
                         }
                     }
-                    if (tid == 0) {
-                        tau_sh[j] = taut;
-                        rdiag[j] = (T)beta;
+                    warp_reduce_to_smem<T, NMAX>(pc, red[warp], lane);
+                    __syncthreads();
+                    // (c) every warp sums the NW partials itself
+                    {
+                        constexpr int K = NMAX >= 32 ? NMAX / 32 : 1;
+#pragma unroll
+                        for (int kk = 0; kk < K; ++kk) {
+                            const int idx = (NMAX >= 32) ? lane * K + kk : lane;
+                            if (idx < NMAX) {
+                                T a = 0;
+#pragma unroll
+                                for (int w = 0; w < NW; ++w) a += red[w][idx];
+                                wfin[warp][idx] = a;
+                                if (warp == 0) {
+                                    const int k = (idx >= past0) ? idx - past0 : ((idx < u) ? base + idx : -1);
+                                    if (k >= 0) Ssh[k][j] = a;
+                                }
+                            }
+                        }
+                        if (tid == 0) {
+                            tau_sh[j] = taut;
+                            rdiag[j] = (T)beta;
+                        }
+                    }
+                    __syncwarp();
+                    // (d) trailing update x_c -= tau (v^T x_c) v over rows >= j
+#pragma unroll
+                    for (int i = 0; i < RPT; ++i) {
+                        const int r = tid + NT * i;
+                        if (r >= j) {
+                            const T tv = taut * ((r == j) ? T(1) : y[i][u]);
+#pragma unroll
+                            for (int c = u + 1; c < NMAX; ++c)
+                                if (c < live) y[i][c] -= tv * wfin[warp][c];
+                        }
                     }
                 }
-                __syncwarp();
-                // (d) trailing update x_c -= tau (v^T x_c) v over rows >= j
+            }
+            // rotate every register row left by U
 #pragma unroll
-                for (int i = 0; i < RPT; ++i) {
-                    const int r = tid + NT * i;
-                    if (r >= j) {
-                        const T tv = taut * ((r == j) ? T(1) : x[i][j]);
+            for (int i = 0; i < RPT; ++i) {
+                T keep[U];
 #pragma unroll
-                        for (int c = j + 1; c < NMAX; ++c) x[i][c] -= tv * wfin[warp][c];
-                    }
-                }
+                for (int u = 0; u < U; ++u) keep[u] = y[i][u];
+#pragma unroll
+                for (int c = 0; c < NMAX - U; ++c) y[i][c] = y[i][c + U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) y[i][NMAX - U + u] = keep[u];
             }
         }
         __syncthreads();  // Ssh, tau_sh, rdiag complete
@@ -214,10 +246,11 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
             T* Rt = p.Rout + t * n;
 #pragma unroll
             for (int c = 0; c < NMAX; ++c) {
-                if (c < n) {
-                    T v = (c > r) ? x[0][c] : ((c == r) ? rdiag[r] : T(0));
+                const int k = (c + shift) % NMAX;
+                if (k < n) {
+                    T v = (k > r) ? y[0][c] : ((k == r) ? rdiag[r] : T(0));
                     if (r >= ht) v = T(0);
-                    Rt[r + c * p.ldr] = v;
+                    Rt[r + k * p.ldr] = v;
                 }
             }
         }
@@ -228,10 +261,8 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
             if (r < ht) {
 #pragma unroll
                 for (int c = 0; c < NMAX; ++c) {
-                    if (c < n) {
-                        const T v = (r > c) ? x[i][c] : Tsh[r][c];
-                        tile[r + c * p.ld] = v;
-                    }
+                    const int k = (c + shift) % NMAX;
+                    if (k < n) tile[r + k * p.ld] = (r > k) ? y[i][c] : Tsh[r][k];
                 }
             }
         }
@@ -239,21 +270,32 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
     }
 }
 
-template <typename T, int NMAX>
+template <typename T, int NMAX, int B>
 constexpr size_t apply_smem_bytes() {
-    return sizeof(T) * (size_t)NMAX * NMAX + 4 * sizeof(T) * (size_t)NMAX * (NMAX + 1);
+    // Vs: the tile (NMAX x B, ld B), Ws: NMAX x NMAX, Vt/Tt/Bs/Ys: NMAX x (NMAX+1)
+    return sizeof(T) * ((size_t)NMAX * B + (size_t)NMAX * NMAX + 4 * (size_t)NMAX * (NMAX + 1));
 }
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 template <typename T, int NMAX, int NT, int RPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) apply_tiles(ApplyParams<T> p) {
     constexpr int B = NT * RPT;
-    // Ws: NMAX x NMAX, then Vt, Tt, Bs, Ys: NMAX x (NMAX+1) each, in dynamic
-    // shared memory (apply_smem_bytes), which can exceed 48 KB.
+    constexpr int VE = 16 / sizeof(T);  // elements per 16-byte copy
     extern __shared__ __align__(16) unsigned char apply_smem[];
     typedef T Row1[NMAX + 1];
     typedef T Row0[NMAX];
-    Row0* Ws = reinterpret_cast<Row0*>(apply_smem);
-    Row1* Vt = reinterpret_cast<Row1*>(apply_smem + sizeof(T) * NMAX * NMAX);
+    T* Vs = reinterpret_cast<T*>(apply_smem);
+    Row0* Ws = reinterpret_cast<Row0*>(Vs + (size_t)NMAX * B);
+    Row1* Vt = reinterpret_cast<Row1*>(Ws + NMAX);
     Row1* Tt = Vt + NMAX;
     Row1* Bs = Tt + NMAX;
     Row1* Ys = Bs + NMAX;
@@ -265,6 +307,27 @@ __global__ void __launch_bounds__(NT, MINB) apply_tiles(ApplyParams<T> p) {
         const int64_t row0 = t * B;
         const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
         T* tile = p.M + row0;
+
+        // Stage the whole tile into shared memory with asynchronous copies;
+        // they land while the top-block products below are computed.
+        if (p.vec) {
+            constexpr int NV = B / VE;
+            for (int e = tid; e < n * NV; e += NT) {
+                const int c = e / NV, r = (e % NV) * VE;
+                if (r + VE <= ht) {
+                    cp_async<16>(Vs + (size_t)c * B + r, tile + r + (int64_t)c * p.ld);
+                } else {
+                    for (int rr = r; rr < ht; ++rr)
+                        cp_async<sizeof(T)>(Vs + (size_t)c * B + rr, tile + rr + (int64_t)c * p.ld);
+                }
+            }
+        } else {
+            for (int e = tid; e < n * B; e += NT) {
+                const int c = e / B, r = e % B;
+                if (r < ht) cp_async<sizeof(T)>(Vs + (size_t)c * B + r, tile + r + (int64_t)c * p.ld);
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
 
         for (int idx = tid; idx < NMAX * NMAX; idx += NT) {
             const int r = idx % NMAX, c = idx / NMAX;
@@ -280,21 +343,24 @@ __global__ void __launch_bounds__(NT, MINB) apply_tiles(ApplyParams<T> p) {
             Bs[r][c] = b;
         }
         __syncthreads();
-        // Y = V_top^T B
+        // Y = V_top^T B (V_top is unit lower triangular: terms r >= k)
         for (int idx = tid; idx < NMAX * NMAX; idx += NT) {
             const int k = idx % NMAX, c = idx / NMAX;
             T a = 0;
-            for (int r = k; r < NMAX; ++r) a += Vt[r][k] * Bs[r][c];
+#pragma unroll
+            for (int r = 0; r < NMAX; ++r) a += Vt[r][k] * Bs[r][c];
             Ys[k][c] = a;
         }
         __syncthreads();
-        // W = T Y
+        // W = T Y (T upper triangular: its zeros make the full sum exact)
         for (int idx = tid; idx < NMAX * NMAX; idx += NT) {
             const int k = idx % NMAX, c = idx / NMAX;
             T a = 0;
-            for (int l = k; l < NMAX; ++l) a += Tt[k][l] * Ys[l][c];
+#pragma unroll
+            for (int l = 0; l < NMAX; ++l) a += Tt[k][l] * Ys[l][c];
             Ws[k][c] = a;
         }
+        cp_async_wait_all();
         __syncthreads();
 
         // Q rows = [B; 0] - V W as n rank-1 updates of the thread's rows.
@@ -305,17 +371,16 @@ __global__ void __launch_bounds__(NT, MINB) apply_tiles(ApplyParams<T> p) {
 #pragma unroll
             for (int c = 0; c < NMAX; ++c) q[i][c] = (r < n) ? Bs[r][c] : T(0);
         }
-#pragma unroll
+#pragma unroll 8
         for (int k = 0; k < NMAX; ++k) {
             if (k < n) {
                 T vk[RPT];
 #pragma unroll
                 for (int i = 0; i < RPT; ++i) {
                     const int r = tid + NT * i;
-                    // rows of the top block come masked from shared memory
-                    // (T above the diagonal, unit diagonal); the rest from
-                    // the tile
-                    vk[i] = (r < n) ? Vt[r][k] : ((r < ht) ? tile[r + k * p.ld] : T(0));
+                    // rows of the top block come masked (T above the
+                    // diagonal, unit diagonal); the rest from the staged tile
+                    vk[i] = (r < n) ? Vt[r][k] : ((r < ht) ? Vs[(size_t)k * B + r] : T(0));
                 }
 #pragma unroll
                 for (int c = 0; c < NMAX; ++c) {
