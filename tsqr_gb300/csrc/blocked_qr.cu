@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 #include "internal.h"
@@ -176,24 +177,56 @@ GemmPlan tn_plan(int64_t M, int64_t N, int64_t K) {
     return {(int)nz, kchunk};
 }
 
-// Workspace layout: [tsqr region | partial sums | reorth temp].
+// Workspace layout: [status word | tsqr region | partial sums | reorth temp].
+// The precision form (FP32, TF32X3) sizes the TSQR region for the
+// precision-form TSQR and the partial sums for the tcgen05 split-K GEMM.
 struct QrWs {
-    size_t tsqr_bytes = 0, part_bytes = 0, tmp_bytes = 0;
-    size_t total() const { return tsqr_bytes + part_bytes + tmp_bytes; }
+    size_t err_bytes = 256, tsqr_bytes = 0, part_bytes = 0, tmp_bytes = 0;
+    size_t total() const { return err_bytes + tsqr_bytes + part_bytes + tmp_bytes; }
 };
 
 template <typename T>
-void qr_ws_walk(int64_t m, int64_t n, int nb, bool reorth, QrWs* w) {
+bool use_tc(const tsqr_opts& o) {
+    return sizeof(T) == 4 && o.precision == TSQR_PRECISION_TF32X3;
+}
+
+template <typename T>
+void qr_ws_walk(int64_t m, int64_t n, int nb, bool reorth, bool tc, QrWs* w) {
     if (n <= nb) {
-        w->tsqr_bytes = std::max(w->tsqr_bytes, (size_t)round_up((int64_t)tsqr_plain_workspace<T>(m, n), 256));
+        const size_t b = tc ? tsqr_precision_workspace(m, n) : tsqr_plain_workspace<T>(m, n);
+        w->tsqr_bytes = std::max(w->tsqr_bytes, (size_t)round_up((int64_t)b, 256));
         return;
     }
     const int64_t n1 = split_of(n, nb), n2 = n - n1;
-    GemmPlan gp = tn_plan(n1, n2, m);
-    w->part_bytes = std::max(w->part_bytes, (size_t)round_up((int64_t)gp.nz * n1 * n2 * (int64_t)sizeof(T), 256));
+    const int64_t nz = tc ? tc_tn_splits(n1, n2, m) : tn_plan(n1, n2, m).nz;
+    w->part_bytes = std::max(w->part_bytes, (size_t)round_up(nz * n1 * n2 * (int64_t)sizeof(T), 256));
     if (reorth) w->tmp_bytes = std::max(w->tmp_bytes, (size_t)round_up(n1 * n2 * (int64_t)sizeof(T), 256));
-    qr_ws_walk<T>(m, n1, nb, reorth, w);
-    qr_ws_walk<T>(m, n2, nb, reorth, w);
+    qr_ws_walk<T>(m, n1, nb, reorth, tc, w);
+    qr_ws_walk<T>(m, n2, nb, reorth, tc, w);
+}
+
+// C (n1 x n2, ldc) = A1^T A2 (+ beta C) on the tensor cores (FP32 only).
+template <typename T>
+void proj_tn_tc(int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2, int64_t lda, T* P, T* C, int64_t ldc,
+                T beta, int* err, cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        const int nz = tc_gemm_tn((int)n1, (int)n2, m, A1, lda, A2, lda, P, err, s);
+        log_launch(kTagTc + 100, s);
+        const int64_t total = n1 * n2;
+        int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 1024);
+        reduce_partials<T><<<blocks, 256, 0, s>>>((int)n1, (int)n2, nz, P, T(1), beta, C, ldc);
+        log_launch(kTagReduce, s);
+    }
+}
+
+// A2 (m x n2) -= A1 (m x n1) X (n1 x n2) on the tensor cores (FP32 only).
+template <typename T>
+void update_nn_tc(int64_t m, int64_t n1, int64_t n2, const T* A1, int64_t lda, const T* X, int64_t ldx, T* A2,
+                  int* err, cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        tc_gemm_nn(m, (int)n2, (int)n1, -1.f, A1, lda, X, ldx, A2, lda, err, s);
+        log_launch(kTagTc + 101, s);
+    }
 }
 
 template <typename T>
@@ -214,25 +247,43 @@ template <typename T>
 tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, char* ws, const QrWs& w,
                    const tsqr_opts& o, cudaStream_t s) {
     const int nb = panel_of(o);
-    if (n <= nb) return tsqr_plain<T>(m, n, A, lda, R, ldr, ws, w.tsqr_bytes, s);
+    const bool tc = use_tc<T>(o);
+    char* tws = ws + w.err_bytes;
+    if (n <= nb) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (tc) return tsqr_precision(m, n, A, lda, R, ldr, tws, w.tsqr_bytes, s);
+        }
+        return tsqr_plain<T>(m, n, A, lda, R, ldr, tws, w.tsqr_bytes, s);
+    }
     const int64_t n1 = split_of(n, nb), n2 = n - n1;
     T* A1 = A;
     T* A2 = A + n1 * lda;
     T* R11 = R;
     T* R12 = R + n1 * ldr;
     T* R22 = R + n1 * ldr + n1;
-    T* P = reinterpret_cast<T*>(ws + w.tsqr_bytes);
-    T* tmp = reinterpret_cast<T*>(ws + w.tsqr_bytes + w.part_bytes);
+    int* err = reinterpret_cast<int*>(ws);
+    T* P = reinterpret_cast<T*>(tws + w.tsqr_bytes);
+    T* tmp = reinterpret_cast<T*>(tws + w.tsqr_bytes + w.part_bytes);
     tsqr_status st = qr_rec<T>(m, n1, A1, lda, R11, ldr, ws, w, o, s);
     if (st != TSQR_OK) return st;
-    proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), s);
     dim3 g((unsigned)ceil_div(m, kTile), (unsigned)ceil_div(n2, kTile));
-    gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, R12, ldr, T(1), A2, lda);
-    log_launch(kTagGemmNN, s);
-    if (o.reorth) {
-        proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), s);
-        gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, tmp, n1, T(1), A2, lda);
+    if (tc) {
+        proj_tn_tc<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), err, s);
+        update_nn_tc<T>(m, n1, n2, A1, lda, R12, ldr, A2, err, s);
+    } else {
+        proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), s);
+        gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, R12, ldr, T(1), A2, lda);
         log_launch(kTagGemmNN, s);
+    }
+    if (o.reorth) {
+        if (tc) {
+            proj_tn_tc<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), err, s);
+            update_nn_tc<T>(m, n1, n2, A1, lda, tmp, n1, A2, err, s);
+        } else {
+            proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), s);
+            gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, tmp, n1, T(1), A2, lda);
+            log_launch(kTagGemmNN, s);
+        }
         int blocks = (int)std::min<int64_t>(ceil_div(n1 * n2, 256), 1024);
         axpy_block<T><<<blocks, 256, 0, s>>>((int)n1, (int)n2, tmp, n1, R12, ldr);
         log_launch(kTagAxpy, s);
@@ -248,7 +299,7 @@ tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, c
 template <typename T>
 size_t qr_workspace(int64_t m, int64_t n, const tsqr_opts& o) {
     QrWs w;
-    qr_ws_walk<T>(m, n, panel_of(o), o.reorth != 0, &w);
+    qr_ws_walk<T>(m, n, panel_of(o), o.reorth != 0, use_tc<T>(o), &w);
     return w.total();
 }
 
@@ -256,8 +307,9 @@ template <typename T>
 tsqr_status qr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
                    const tsqr_opts& o, cudaStream_t s) {
     QrWs w;
-    qr_ws_walk<T>(m, n, panel_of(o), o.reorth != 0, &w);
+    qr_ws_walk<T>(m, n, panel_of(o), o.reorth != 0, use_tc<T>(o), &w);
     if (work == nullptr || work_bytes < w.total()) return TSQR_ERR_WORKSPACE;
+    if (use_tc<T>(o) && cudaMemsetAsync(work, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
     return qr_rec<T>(m, n, A, lda, R, ldr, reinterpret_cast<char*>(work), w, o, s);
 }
 

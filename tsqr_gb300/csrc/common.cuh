@@ -57,6 +57,36 @@ __device__ __forceinline__ void warp_reduce_to_smem(T (&p)[NV], T* row, int lane
     }
 }
 
+// Same result as warp_reduce_to_smem, through a per-warp shared-memory
+// transpose instead of shuffles: every lane stores its NV partials as one
+// padded row (16-byte stores), then lane l sums column l (and l + 32 for
+// NV = 64).  The row stride NV + 4 keeps both the row stores and the column
+// loads free of bank conflicts.  About 8 + 32 + 31 instructions per lane for
+// NV = 32 instead of 31 shuffles, 31 adds and 62 selects.  FP32 only.
+template <int NV>
+__host__ __device__ constexpr int xpose_stride() {
+    return NV + 4;
+}
+template <int NV>
+__device__ __forceinline__ void warp_reduce_to_smem_x(float (&p)[NV], float* row, float* scratch, int lane) {
+    constexpr int SP = xpose_stride<NV>();
+    float* mine = scratch + lane * SP;
+#pragma unroll
+    for (int c = 0; c < NV; c += 4) *reinterpret_cast<float4*>(mine + c) = make_float4(p[c], p[c + 1], p[c + 2], p[c + 3]);
+    __syncwarp();
+#pragma unroll
+    for (int half = 0; half < (NV + 31) / 32; ++half) {
+        const int idx = lane + 32 * half;
+        if (idx < NV) {
+            float a = 0.f;
+#pragma unroll
+            for (int r = 0; r < 32; ++r) a += scratch[r * SP + idx];
+            row[idx] = a;
+        }
+    }
+    __syncwarp();
+}
+
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 __host__ __device__ inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
 

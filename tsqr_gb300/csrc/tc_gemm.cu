@@ -1,0 +1,278 @@
+// tc_gemm.cu -- the blocked-QR trailing GEMMs on the tcgen05 tensor cores
+// (precision form of qr<float>, block_QR.h:72-95).
+//
+// The reference's naive gemm_blockqr (block_QR.h:7-60) computes
+//   R12 = A1^T A2      (op = T, a length-m dot per thread) and
+//   A2  = A2 - A1 R12  (op = N).
+// Here both run as tcgen05.mma kind::tf32 with FP32 accumulation in TMEM and
+// the operands split into TF32 hi + lo (three products hi*hi + hi*lo +
+// lo*hi, about 2^-21 relative per product).
+//
+// tc_gemm_kernel<TRANS_A>: a CTA of 128 threads owns a 128 x NB block of the
+// output (TMEM lanes = output rows, NB fp32 columns) and walks its K range
+// in stages of 32.  Per stage every thread loads its share of the A and B
+// slices, splits them and stores the K-major operand tiles; one thread
+// issues 3 x 4 MMAs (M = 128, N = NB, K = 8) and commits them to the stage's
+// mbarrier.  Two stage buffers alternate, so the loads of stage s+1 overlap
+// the MMAs of stage s.
+//   TRANS_A = true : D = A^T B over rows [k0, k1) of A (K x M) and B (K x N)
+//                    -> written as a partial sum P_z (M x N), summed later
+//                    (deterministic split-K, no atomics).
+//   TRANS_A = false: D = A B with A (M x K) and B (K x N) small
+//                    -> C = C + alpha * D.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "internal.h"
+#include "tc.cuh"
+
+namespace tsqr {
+
+namespace {
+
+constexpr int KS = 32;  // K per stage
+
+template <int NB>
+struct GemmSmem {
+    uint32_t a_hi[2][128 * KS];
+    uint32_t a_lo[2][128 * KS];
+    uint32_t b_hi[2][NB * KS];
+    uint32_t b_lo[2][NB * KS];
+    unsigned long long mbar[2];
+    uint32_t tmem_slot;
+};
+
+template <bool TRANS_A, int NB>
+__global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, const float* __restrict__ A, int64_t lda,
+                                                      const float* __restrict__ Bm, int64_t ldb, float* C, int64_t ldc,
+                                                      float alpha, int64_t kchunk, int* err) {
+    extern __shared__ __align__(1024) unsigned char gemm_smem_raw[];
+    GemmSmem<NB>& S = *reinterpret_cast<GemmSmem<NB>*>(gemm_smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    constexpr uint32_t idesc = tc::idesc_tf32(128, NB);
+    constexpr uint32_t SBO = KS * 32;  // bytes per 8-row group of a K-major tile with K = KS
+
+    const int m0 = blockIdx.x * 128;
+    const int n0 = blockIdx.y * NB;
+    const int64_t kbeg = TRANS_A ? (int64_t)blockIdx.z * kchunk : 0;
+    const int64_t kend = TRANS_A ? (K < kbeg + kchunk ? K : kbeg + kchunk) : K;
+    const int nstage = (int)((kend - kbeg + KS - 1) / KS);
+
+    if (warp == 0) tc::tmem_alloc(&S.tmem_slot, NB);
+    if (tid == 0) {
+        tc::mbar_init(tc::smem_u32(&S.mbar[0]), 1);
+        tc::mbar_init(tc::smem_u32(&S.mbar[1]), 1);
+        tc::fence_mbar_init();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = S.tmem_slot;
+    uint32_t phase_bits = 0u;  // bit b: phase of mbar[b]
+    bool ok = true;
+
+    // Stage s: K rows [k0, k0 + KS).  A operand rows = output rows m, B
+    // operand rows = output columns n, both K-major (KS values per row).
+    auto stage = [&](int s, int buf) {
+        const int64_t k0 = kbeg + (int64_t)s * KS;
+        unsigned char* ah = reinterpret_cast<unsigned char*>(S.a_hi[buf]);
+        unsigned char* al = reinterpret_cast<unsigned char*>(S.a_lo[buf]);
+        unsigned char* bh = reinterpret_cast<unsigned char*>(S.b_hi[buf]);
+        unsigned char* bl = reinterpret_cast<unsigned char*>(S.b_lo[buf]);
+        // A: 128 rows x KS.  Each task = one row, 4 consecutive k.  When K
+        // is contiguous in global memory (A^T), 8 neighbouring threads take
+        // 8 rows of the same 16-byte K chunk (one 128-byte row of core
+        // matrices: conflict-free stores) and 4 such groups cover 64
+        // contiguous bytes of each row's column (full sectors).
+        for (int task = tid; task < 128 * (KS / 4); task += 128) {
+            int row, k4;
+            if (TRANS_A) {
+                const int grp = task >> 5;
+                row = (grp % 16) * 8 + (task & 7);
+                k4 = ((grp / 16) * 4 + ((task >> 3) & 3)) * 4;
+            } else {  // consecutive threads take consecutive rows of A
+                row = task % 128;
+                k4 = (task / 128) * 4;
+            }
+            float v[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int64_t k = k0 + k4 + e;
+                const int m = m0 + row;
+                float x = 0.f;
+                if (k < kend && m < M) x = TRANS_A ? A[k + (int64_t)m * lda] : A[m + k * lda];
+                v[e] = x;
+            }
+            uint4 hi, lo;
+            tc::split_tf32(v[0], hi.x, lo.x);
+            tc::split_tf32(v[1], hi.y, lo.y);
+            tc::split_tf32(v[2], hi.z, lo.z);
+            tc::split_tf32(v[3], hi.w, lo.w);
+            const uint32_t off = tc::kmajor_off(row, k4, KS);
+            *reinterpret_cast<uint4*>(ah + off) = hi;
+            *reinterpret_cast<uint4*>(al + off) = lo;
+        }
+        // B: NB rows (output columns) x KS; element (n, k) = Bm[k + n*ldb].
+        for (int task = tid; task < NB * (KS / 4); task += 128) {
+            const int grp = task >> 5;
+            const int row = (grp % (NB / 8)) * 8 + (task & 7);
+            const int k4 = ((grp / (NB / 8)) * 4 + ((task >> 3) & 3)) * 4;
+            float v[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int64_t k = k0 + k4 + e;
+                const int nn = n0 + row;
+                v[e] = (k < kend && nn < N) ? Bm[k + (int64_t)nn * ldb] : 0.f;
+            }
+            uint4 hi, lo;
+            tc::split_tf32(v[0], hi.x, lo.x);
+            tc::split_tf32(v[1], hi.y, lo.y);
+            tc::split_tf32(v[2], hi.z, lo.z);
+            tc::split_tf32(v[3], hi.w, lo.w);
+            const uint32_t off = tc::kmajor_off(row, k4, KS);
+            *reinterpret_cast<uint4*>(bh + off) = hi;
+            *reinterpret_cast<uint4*>(bl + off) = lo;
+        }
+        tc::fence_smem_to_async();
+    };
+    auto issue = [&](int s, int buf) {
+        const uint32_t ah = tc::smem_u32(S.a_hi[buf]), al = tc::smem_u32(S.a_lo[buf]);
+        const uint32_t bh = tc::smem_u32(S.b_hi[buf]), bl = tc::smem_u32(S.b_lo[buf]);
+#pragma unroll
+        for (int ks = 0; ks < KS / 8; ++ks) {
+            const uint32_t ko = ks * 256;
+            const uint64_t dah = tc::smem_desc(ah + ko, 128, SBO), dal = tc::smem_desc(al + ko, 128, SBO);
+            const uint64_t dbh = tc::smem_desc(bh + ko, 128, SBO), dbl = tc::smem_desc(bl + ko, 128, SBO);
+            tc::mma_tf32(tmem, dah, dbh, idesc, (s > 0) || (ks > 0));
+            tc::mma_tf32(tmem, dah, dbl, idesc, true);
+            tc::mma_tf32(tmem, dal, dbh, idesc, true);
+        }
+        tc::mma_commit(tc::smem_u32(&S.mbar[buf]));
+    };
+
+    if (nstage > 0) stage(0, 0);
+    for (int s = 0; s < nstage && ok; ++s) {
+        const int buf = s & 1;
+        tc::fence_before_sync();
+        __syncthreads();  // stage s is in shared memory
+        if (tid == 0) {
+            tc::fence_after_sync();
+            issue(s, buf);
+        }
+        if (s + 1 < nstage) {
+            // buffer buf^1 was read by the MMAs of stage s-1: wait for them
+            bool waited = true;
+            if (s >= 1) {
+                waited = tc::mbar_wait(tc::smem_u32(&S.mbar[buf ^ 1]), (phase_bits >> (buf ^ 1)) & 1u);
+                phase_bits ^= 1u << (buf ^ 1);
+            }
+            if (__syncthreads_or(!waited)) {
+                ok = false;
+                break;
+            }
+            stage(s + 1, buf ^ 1);
+        }
+    }
+    // wait for the last two stages' MMAs (in order of commit)
+    if (ok && nstage > 0) {
+        bool waited = true;
+        if (nstage >= 2) {
+            const int b = (nstage - 2) & 1;
+            waited = tc::mbar_wait(tc::smem_u32(&S.mbar[b]), (phase_bits >> b) & 1u);
+            phase_bits ^= 1u << b;
+        }
+        const int b = (nstage - 1) & 1;
+        waited = tc::mbar_wait(tc::smem_u32(&S.mbar[b]), (phase_bits >> b) & 1u) && waited;
+        phase_bits ^= 1u << b;
+        if (__syncthreads_or(!waited)) ok = false;
+    }
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+    } else {
+        tc::fence_after_sync();
+        const int m = m0 + 32 * warp + (tid & 31);
+        float* Cz = TRANS_A ? C + (int64_t)blockIdx.z * M * N : C;
+        const int64_t ldz = TRANS_A ? M : ldc;
+#pragma unroll 1
+        for (int c8 = 0; c8 < NB; c8 += 8) {
+            float d[8];
+            tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c8, d);
+            tc::tmem_ld_wait();
+            if (m < M) {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int nn = n0 + c8 + e;
+                    if (nn < N) {
+                        float* dst = Cz + m + (int64_t)nn * ldz;
+                        if (TRANS_A)
+                            *dst = nstage > 0 ? d[e] : 0.f;
+                        else if (nstage > 0)
+                            *dst = *dst + alpha * d[e];
+                    }
+                }
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, NB);
+}
+
+template <bool TRANS_A, int NB>
+void launch_gemm(dim3 grid, int M, int N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
+                 float* C, int64_t ldc, float alpha, int64_t kchunk, int* err, cudaStream_t s) {
+    constexpr size_t smem = sizeof(GemmSmem<NB>) + 1024;
+    static bool attr = [] {
+        return cudaFuncSetAttribute(tc_gemm_kernel<TRANS_A, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem) == cudaSuccess;
+    }();
+    (void)attr;
+    tc_gemm_kernel<TRANS_A, NB><<<grid, 128, smem, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err);
+}
+
+int nb_for(int N) { return N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256)); }
+
+}  // namespace
+
+int tc_tn_splits(int64_t M, int64_t N, int64_t K) {
+    const int64_t tiles = ((M + 127) / 128) * ((N + 255) / 256);
+    int64_t nz = std::max<int64_t>(1, (2 * 152 + tiles - 1) / tiles);
+    nz = std::min<int64_t>(nz, std::max<int64_t>(1, K / 1024));
+    return (int)nz;
+}
+
+// P_z = A^T B over K-chunks (M, N <= 256 per launch dimension); P holds
+// nz * M * N floats.  Returns the number of partial sums written.
+int tc_gemm_tn(int M, int N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb, float* P, int* err,
+               cudaStream_t s) {
+    const int nz = tc_tn_splits(M, N, K);
+    int64_t kchunk = (K + nz - 1) / nz;
+    kchunk = (kchunk + KS - 1) / KS * KS;
+    const int nzr = (int)((K + kchunk - 1) / kchunk);
+    const int nb = nb_for(std::min(N, 256));
+    dim3 g((unsigned)((M + 127) / 128), (unsigned)((N + nb - 1) / nb), (unsigned)nzr);
+    switch (nb) {
+        case 32: launch_gemm<true, 32>(g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s); break;
+        case 64: launch_gemm<true, 64>(g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s); break;
+        case 128: launch_gemm<true, 128>(g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s); break;
+        default: launch_gemm<true, 256>(g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s); break;
+    }
+    return nzr;
+}
+
+// C (M x N) += alpha * A (M x K) * B (K x N), K and N small (<= 256 per N block).
+void tc_gemm_nn(int64_t M, int N, int K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb,
+                float* C, int64_t ldc, int* err, cudaStream_t s) {
+    const int nb = nb_for(std::min(N, 256));
+    dim3 g((unsigned)((M + 127) / 128), (unsigned)((N + nb - 1) / nb), 1);
+    switch (nb) {
+        case 32: launch_gemm<false, 32>(g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s); break;
+        case 64: launch_gemm<false, 64>(g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s); break;
+        case 128: launch_gemm<false, 128>(g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s); break;
+        default: launch_gemm<false, 256>(g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s); break;
+    }
+}
+
+}  // namespace tsqr

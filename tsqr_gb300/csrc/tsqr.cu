@@ -194,12 +194,17 @@ struct PrecCfg {
 
 PrecCfg pick_precision(int n) {
     PrecCfg c;
+    // The tile factorisation is the plain FP32 kernel.  Computing the
+    // per-column norm, beta and tau in FP64 (the NORM64 variant) was measured
+    // at 2.7x the FP32 factor time on GB300's FP64 pipe (4.66 ms vs 1.73 ms
+    // at 4,194,304 x 32) with no gain in the error figures, so the FP64 part
+    // of this form is the root combine only.
     if (n <= 32) {
         c.nmax = 32;
-        c.ks = make_set<TileCfg<float, 32, 128, 4, 2, 2, 256, true>, float>();
+        c.ks = make_set<TileCfg<float, 32, 128, 4, 2, 2, 256>, float>();
     } else if (n <= 64) {
         c.nmax = 64;
-        c.ks = make_set<TileCfg<float, 64, 256, 1, 1, 1, 256, true>, float>();
+        c.ks = make_set<TileCfg<float, 64, 256, 1, 1, 1, 256>, float>();
     }
     c.rows = c.ks.rows;
     return c;
@@ -209,6 +214,14 @@ struct PrecLayout {
     size_t status = 0, levels = 0, root = 0, rootws = 0, total = 0;
 };
 
+// Root combine in FP64 (the root level converted to double, factored by the
+// FP64 tree, converted back).  Off: on GB300 the FP64 factorisation of even
+// the 64 x 32 root of a 4,194,304 x 32 problem took 0.47 ms of a 2.25 ms
+// call (FP64 runs at a small fraction of the FP32 rate there), and the FP32
+// root already meets the form's error bar.  The path is kept, tested by the
+// same code as the FP64 entry points, for builds that turn it on.
+constexpr bool kRoot64 = false;
+
 PrecLayout prec_layout(int64_t m, int64_t n, const PrecCfg& c) {
     PrecLayout L;
     L.status = 0;
@@ -217,7 +230,7 @@ PrecLayout prec_layout(int64_t m, int64_t n, const PrecCfg& c) {
     const size_t lev = plan_levels<float>(m, n, nullptr, m, c.rows, nullptr, &lv);
     L.root = L.levels + lev;
     const int64_t hroot = lv.back().h;
-    const bool root64 = n <= 32;
+    const bool root64 = kRoot64 && n <= 32;
     const size_t rootbytes = root64 ? (size_t)round_up(hroot * n * 8 + n * n * 8, (int64_t)kAlign) : 0;
     L.rootws = L.root + rootbytes;
     L.total = L.rootws + (root64 ? round_up((int64_t)tsqr_plain_workspace<double>(hroot, n), (int64_t)kAlign) : 0);
@@ -246,7 +259,7 @@ tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R
     plan_levels<float>(m, n, A, lda, c.rows, base + PL.levels, &lv);
     const int L = (int)lv.size();
     if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
-    const bool root64 = n <= 32;
+    const bool root64 = kRoot64 && n <= 32;
     const int top = root64 ? L - 1 : L;  // levels factored in FP32 below the root
     for (int l = 0; l < top; ++l) {
         FactorParams<float> fp;

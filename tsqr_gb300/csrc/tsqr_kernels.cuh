@@ -65,32 +65,49 @@ struct ApplyParams {
     int vec;        // 1: ld and the level base allow 16-byte copies
 };
 
-template <typename T, int NMAX, int NT, int RPT, int MINB, bool NORM64>
-__global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
+// Shared memory of one factor CTA.
+template <typename T, int NMAX, int NT, bool NORM64>
+struct FactorSmem {
+    static constexpr int NW = NT / 32;
+    using N64 = typename std::conditional<NORM64, double, T>::type;
+    N64 s_part[NW];
+    T s_alpha;
+    T red[NW][NMAX];
+    __align__(16) T wfin[NW][NMAX];
+    T Ssh[NMAX][NMAX + 1];
+    T Tsh[NMAX][NMAX + 1];
+    T tau_sh[NMAX];
+    T rdiag[NMAX];
+    // per-warp transpose scratch of the FP32 dot-product reduction
+    __align__(16) float xpose[std::is_same<T, float>::value ? NW : 1]
+                             [std::is_same<T, float>::value ? 32 * xpose_stride<NMAX>() : 4];
+};
+
+// Householder QR of one tile: ht (<= NT*RPT) rows of n columns at `tile`
+// (leading dimension ld), factored in place (V below the diagonal, T in the
+// top block's upper triangle); its n x n R goes to Rt (leading dimension
+// ldr).  Called by every thread of the CTA.
+template <typename T, int NMAX, int NT, int RPT, bool NORM64>
+__device__ __forceinline__ void factor_tile(FactorSmem<T, NMAX, NT, NORM64>& S, T* tile, int64_t ld, int ht, int n,
+                                            T* Rt, int64_t ldr) {
     constexpr int NW = NT / 32;
-    constexpr int B = NT * RPT;
     constexpr int U = 4;  // columns per unrolled group
     static_assert(NT >= NMAX && NT % 32 == 0 && NMAX % U == 0, "bad tile configuration");
-    using N64 = typename std::conditional<NORM64, double, T>::type;
-    __shared__ N64 s_part[NW];
-    __shared__ T s_alpha;
-    __shared__ T red[NW][NMAX];
-    __shared__ __align__(16) T wfin[NW][NMAX];
-    __shared__ T Ssh[NMAX][NMAX + 1];
-    __shared__ T Tsh[NMAX][NMAX + 1];
-    __shared__ T tau_sh[NMAX];
-    __shared__ T rdiag[NMAX];
+    using N64 = typename FactorSmem<T, NMAX, NT, NORM64>::N64;
+    auto& s_part = S.s_part;
+    auto& s_alpha = S.s_alpha;
+    auto& red = S.red;
+    auto& wfin = S.wfin;
+    auto& Ssh = S.Ssh;
+    auto& Tsh = S.Tsh;
+    auto& tau_sh = S.tau_sh;
+    auto& rdiag = S.rdiag;
+    auto& xpose = S.xpose;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int n = p.n;
     const int G = (n + U - 1) / U;
     const int shift = (U * G) % NMAX;  // register position c ends up holding column (c + shift) % NMAX
-
-    for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-        const int64_t row0 = t * B;
-        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
-        T* tile = p.M + row0;
-
+    {
         // y[i][c]: row tid + NT*i.  The column loop runs in groups of U
         // columns; after each group the register row rotates left by U, so at
         // group g position c < n - U*g holds column U*g + c (positions 0..U-1
@@ -103,7 +120,7 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
             const int r = tid + NT * i;
 #pragma unroll
             for (int c = 0; c < NMAX; ++c)
-                y[i][c] = (r < ht && c < n) ? tile[r + c * p.ld] : T(0);
+                y[i][c] = (r < ht && c < n) ? tile[r + c * ld] : T(0);
         }
 
 #pragma unroll 1
@@ -115,13 +132,15 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
             for (int u = 0; u < U; ++u) {
                 const int j = base + u;
                 if (j < n) {
+                    // Row slots i >= 1 hold rows >= NT >= NMAX > j, so only
+                    // slot 0 needs the row-versus-diagonal tests below.
                     // (a) sigma^2 = ||x(j+1:, j)||^2 and alpha = x(j, j)
                     N64 s = 0;
 #pragma unroll
                     for (int i = 0; i < RPT; ++i) {
                         const int r = tid + NT * i;
-                        if (r > j) s += (N64)y[i][u] * (N64)y[i][u];
-                        if (r == j) s_alpha = y[i][u];
+                        if (i > 0 || r > j) s += (N64)y[i][u] * (N64)y[i][u];
+                        if (i == 0 && r == j) s_alpha = y[i][u];
                     }
                     s = warp_sum(s);
                     if (lane == 0) s_part[warp] = s;
@@ -149,24 +168,28 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
 #pragma unroll
                     for (int i = 0; i < RPT; ++i) {
                         const int r = tid + NT * i;
-                        if (r > j) y[i][u] *= scalet;
+                        if (i > 0 || r > j) y[i][u] *= scalet;
                     }
+                    // v of slot 0: 0 above the diagonal, 1 on it
+                    const T v0 = (tid > j) ? y[0][u] : ((tid == j) ? T(1) : T(0));
                     T pc[NMAX];
 #pragma unroll
-                    for (int c = 0; c < NMAX; ++c) pc[c] = 0;
+                    for (int c = 0; c < NMAX; ++c) pc[c] = (c != u) ? v0 * y[0][c] : T(0);
 #pragma unroll
-                    for (int i = 0; i < RPT; ++i) {
-                        const int r = tid + NT * i;
-                        if (r >= j) {
-                            const T v = (r == j) ? T(1) : y[i][u];
+                    for (int i = 1; i < RPT; ++i) {
+                        const T v = y[i][u];
 #pragma unroll
-                            for (int c = 0; c < NMAX; ++c)
-                                if (c != u) pc[c] += v * y[i][c];
-                        }
+                        for (int c = 0; c < NMAX; ++c)
+                            if (c != u) pc[c] += v * y[i][c];
                     }
-                    warp_reduce_to_smem<T, NMAX>(pc, red[warp], lane);
+                    if constexpr (std::is_same<T, float>::value)
+                        warp_reduce_to_smem_x<NMAX>(pc, red[warp], xpose[warp], lane);
+                    else
+                        warp_reduce_to_smem<T, NMAX>(pc, red[warp], lane);
                     __syncthreads();
-                    // (c) every warp sums the NW partials itself
+                    // (c) every warp sums the NW partials itself; positions
+                    // that are not trailing columns get a zero coefficient, so
+                    // the update below needs no per-column test
                     {
                         constexpr int K = NMAX >= 32 ? NMAX / 32 : 1;
 #pragma unroll
@@ -176,7 +199,7 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
                                 T a = 0;
 #pragma unroll
                                 for (int w = 0; w < NW; ++w) a += red[w][idx];
-                                wfin[warp][idx] = a;
+                                wfin[warp][idx] = (idx > u && idx < live) ? a : T(0);
                                 if (warp == 0) {
                                     const int k = (idx >= past0) ? idx - past0 : ((idx < u) ? base + idx : -1);
                                     if (k >= 0) Ssh[k][j] = a;
@@ -189,16 +212,16 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
                         }
                     }
                     __syncwarp();
-                    // (d) trailing update x_c -= tau (v^T x_c) v over rows >= j
+                    // (d) trailing update x_c -= tau (v^T x_c) v (v = 0 above
+                    // the diagonal, coefficient 0 off the trailing columns)
+                    T wr[NMAX];
+#pragma unroll
+                    for (int c = 0; c < NMAX; ++c) wr[c] = wfin[warp][c];
 #pragma unroll
                     for (int i = 0; i < RPT; ++i) {
-                        const int r = tid + NT * i;
-                        if (r >= j) {
-                            const T tv = taut * ((r == j) ? T(1) : y[i][u]);
+                        const T tv = taut * ((i > 0) ? y[i][u] : v0);
 #pragma unroll
-                            for (int c = u + 1; c < NMAX; ++c)
-                                if (c < live) y[i][c] -= tv * wfin[warp][c];
-                        }
+                        for (int c = u + 1; c < NMAX; ++c) y[i][c] -= tv * wr[c];
                     }
                 }
             }
@@ -243,14 +266,13 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
         // R of this tile: row r < n is held by thread r (i = 0).
         if (tid < n) {
             const int r = tid;
-            T* Rt = p.Rout + t * n;
 #pragma unroll
             for (int c = 0; c < NMAX; ++c) {
                 const int k = (c + shift) % NMAX;
                 if (k < n) {
                     T v = (k > r) ? y[0][c] : ((k == r) ? rdiag[r] : T(0));
                     if (r >= ht) v = T(0);
-                    Rt[r + k * p.ldr] = v;
+                    Rt[r + k * ldr] = v;
                 }
             }
         }
@@ -262,11 +284,22 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
 #pragma unroll
                 for (int c = 0; c < NMAX; ++c) {
                     const int k = (c + shift) % NMAX;
-                    if (k < n) tile[r + k * p.ld] = (r > k) ? y[i][c] : Tsh[r][k];
+                    if (k < n) tile[r + k * ld] = (r > k) ? y[i][c] : Tsh[r][k];
                 }
             }
         }
         __syncthreads();
+    }
+}
+
+template <typename T, int NMAX, int NT, int RPT, int MINB, bool NORM64>
+__global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
+    constexpr int B = NT * RPT;
+    __shared__ FactorSmem<T, NMAX, NT, NORM64> S;
+    for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        const int64_t row0 = t * B;
+        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
+        factor_tile<T, NMAX, NT, RPT, NORM64>(S, p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n, p.ldr);
     }
 }
 
@@ -286,11 +319,16 @@ __device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-template <typename T, int NMAX, int NT, int RPT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) apply_tiles(ApplyParams<T> p) {
+// Q assembly of one tile: ht (<= NT*RPT) rows of n columns at `tile` (ld),
+// holding V and T from factor_tile, overwritten by (I - V T V^T) [B; 0]
+// where B is the n x n block at Pb (leading dimension ldp), or the identity
+// when Pb is null.  vec: 16-byte copies are legal (ld and tile aligned).
+// smem: apply_smem_bytes<T, NMAX, NT*RPT>() bytes.  Called by every thread.
+template <typename T, int NMAX, int NT, int RPT>
+__device__ __forceinline__ void apply_tile(unsigned char* apply_smem, T* tile, int64_t ld, int ht, int n,
+                                           const T* Pb, int64_t ldp, int vec) {
     constexpr int B = NT * RPT;
     constexpr int VE = 16 / sizeof(T);  // elements per 16-byte copy
-    extern __shared__ __align__(16) unsigned char apply_smem[];
     typedef T Row1[NMAX + 1];
     typedef T Row0[NMAX];
     T* Vs = reinterpret_cast<T*>(apply_smem);
@@ -299,15 +337,14 @@ __global__ void __launch_bounds__(NT, MINB) apply_tiles(ApplyParams<T> p) {
     Row1* Tt = Vt + NMAX;
     Row1* Bs = Tt + NMAX;
     Row1* Ys = Bs + NMAX;
-
     const int tid = threadIdx.x;
-    const int n = p.n;
-
-    for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-        const int64_t row0 = t * B;
-        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
-        T* tile = p.M + row0;
-
+    struct {
+        int64_t ld, ldp;
+        const T* P;
+        int vec;
+    } p = {ld, ldp, Pb, vec};
+    const int64_t t = 0;  // Pb already points at this tile's block
+    {
         // Stage the whole tile into shared memory with asynchronous copies;
         // they land while the top-block products below are computed.
         if (p.vec) {
@@ -400,6 +437,18 @@ __global__ void __launch_bounds__(NT, MINB) apply_tiles(ApplyParams<T> p) {
             }
         }
         __syncthreads();
+    }
+}
+
+template <typename T, int NMAX, int NT, int RPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) apply_tiles(ApplyParams<T> p) {
+    constexpr int B = NT * RPT;
+    extern __shared__ __align__(16) unsigned char apply_smem[];
+    for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        const int64_t row0 = t * B;
+        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
+        apply_tile<T, NMAX, NT, RPT>(apply_smem, p.M + row0, p.ld, ht, p.n, p.P ? p.P + t * p.n : nullptr, p.ldp,
+                                     p.vec);
     }
 }
 
