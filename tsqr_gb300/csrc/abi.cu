@@ -133,18 +133,26 @@ tsqr_status qr_double(int m, int n, double* A, int lda, double* R, int ldr, doub
 }
 
 size_t tsqr_batched_workspace_bytes(int count, const int64_t* m, const int64_t* n) {
-    (void)count;
-    (void)m;
-    (void)n;
-    return 0;
+    if (count < 0 || (count > 0 && (m == nullptr || n == nullptr))) return 0;
+    return tsqr::batched_workspace(count, m, n);
 }
 
 tsqr_status tsqr_batched_s(int count, float* const* A, const int64_t* m, const int64_t* n, const int64_t* lda,
                            float* const* R, const int64_t* ldr, void* work, size_t work_bytes,
                            const tsqr_opts* opts, void* stream) {
-    (void)count; (void)A; (void)m; (void)n; (void)lda; (void)R; (void)ldr;
-    (void)work; (void)work_bytes; (void)opts; (void)stream;
-    return TSQR_ERR_UNSUPPORTED;
+    const tsqr_opts o = opts_or_default(opts);
+    if (count < 0) return TSQR_ERR_INVALID_ARG;
+    if (count == 0) return TSQR_OK;
+    if (!A || !m || !n || !lda || !R || !ldr) return TSQR_ERR_INVALID_ARG;
+    for (int i = 0; i < 5; ++i)
+        if (o.reserved[i] != 0) return TSQR_ERR_INVALID_ARG;
+    if (o.precision != TSQR_PRECISION_PLAIN) return TSQR_ERR_UNSUPPORTED;
+    for (int i = 0; i < count; ++i) {
+        if (m[i] < 1 || n[i] < 1 || m[i] < n[i] || lda[i] < m[i] || ldr[i] < n[i]) return TSQR_ERR_INVALID_ARG;
+        if (A[i] == nullptr || R[i] == nullptr) return TSQR_ERR_INVALID_ARG;
+        if (n[i] > 64 || m[i] > INT32_MAX) return TSQR_ERR_UNSUPPORTED;
+    }
+    return tsqr::batched_run(count, A, m, n, lda, R, ldr, work, work_bytes, (cudaStream_t)stream);
 }
 
 const char* tsqr_status_string(tsqr_status s) {

@@ -62,3 +62,10 @@ int tc_gemm_tn(int M, int N, int64_t K, const float* A, int64_t lda, const float
 void tc_gemm_nn(int64_t M, int N, int K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb,
                 float* C, int64_t ldc, int* err, cudaStream_t s);
 }  // namespace tsqr
+
+namespace tsqr {
+// Batched TSQR (batched.cu), FP32, n <= 64.
+size_t batched_workspace(int count, const int64_t* m, const int64_t* n);
+tsqr_status batched_run(int count, float* const* A, const int64_t* m, const int64_t* n, const int64_t* lda,
+                        float* const* R, const int64_t* ldr, void* work, size_t work_bytes, cudaStream_t s);
+}  // namespace tsqr
