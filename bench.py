@@ -248,6 +248,70 @@ def cpu_lapack(m, n, seed=0):
             "kind": "lapack sgeqrf+sorgqr (OpenBLAS via scipy)", "seconds": sec}
 
 
+def run_batch(tg, steps, warmup, device, seed=2024):
+    """512 FP32 problems, heights log-uniform in [2048, 262144], widths from
+    {8, 16, 32, 64}, entries uniform[-1, 1): the batched entry point captured
+    once into a CUDA graph and replayed, against a loop of the single-problem
+    entry point over the same matrices.  Inputs restored before every step
+    (outside the timed pair)."""
+    import ctypes
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(seed)
+    ms = np.exp(rng.uniform(np.log(2048), np.log(262144), 512)).astype(np.int64)
+    ns = rng.choice([8, 16, 32, 64], 512)
+    g = torch.Generator(device=device).manual_seed(seed)
+    A0 = [torch.rand((int(n), int(m)), generator=g, device=device).mul_(2).sub_(1).t() for m, n in zip(ms, ns)]
+    As = [a.t().clone().t() for a in A0]
+    Rs = [tg.empty_colmajor(int(n), int(n), torch.float32, device) for n in ns]
+    c = len(As)
+    i64 = ctypes.c_int64 * c
+    nbytes = tg.lib().tsqr_batched_workspace_bytes(c, i64(*[int(x) for x in ms]), i64(*[int(x) for x in ns]))
+    work = torch.empty(nbytes, dtype=torch.uint8, device=device)
+    F = float(sum(flops(int(m), int(n)) for m, n in zip(ms, ns)))
+    stream = torch.cuda.Stream(device=device)
+
+    def restore():
+        for a, b in zip(As, A0):
+            a.copy_(b)
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(warmup, 1)):
+            restore()
+            tg.tsqr_batched_(As, Rs, work=work, stream=stream)
+    stream.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        tg.tsqr_batched_(As, Rs, work=work, stream=stream)
+    out = {}
+    for mode in ("batched_graph", "loop_single"):
+        ts = []
+        for k in range(warmup + steps):
+            with torch.cuda.stream(stream):
+                restore()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                if mode == "batched_graph":
+                    graph.replay()
+                else:
+                    for x, r in zip(As, Rs):
+                        tg.tsqr_(x, r, stream=stream)
+                b.record(stream)
+            stream.synchronize()
+            if k >= warmup:
+                ts.append(a.elapsed_time(b))
+        msx = sum(ts) / len(ts)
+        out[mode] = {"ms": msx, "problems_per_s": 512 / (msx * 1e-3), "tflops": F / (msx * 1e-3) / 1e12}
+    back = []
+    for k in range(0, 512, 64):
+        a0, q, r = A0[k].double(), As[k].double(), Rs[k].double()
+        back.append((torch.linalg.norm(a0 - q @ r) / torch.linalg.norm(a0)).item())
+    out["max_backward_sampled"] = max(back)
+    out["rows"] = int(ms.sum())
+    out["flops"] = F
+    return out
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -265,6 +329,7 @@ def main():
     ap.add_argument("--n", type=int, default=32)
     ap.add_argument("--form", default="auto")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="tsqr", choices=["tsqr", "batch"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
@@ -311,6 +376,23 @@ def main():
     pk = peaks()
     sms = torch.cuda.get_device_properties(device).multi_processor_count
     fp32_peak = sms * 128 * 2 * pk["sm_max_mhz"] * 1e6 / 1e12
+
+    if args.workload == "batch":
+        sampler = ClockSampler(local)
+        sampler.start()
+        res = run_batch(tg, args.steps, args.warmup, device)
+        clocks = sampler.stop()
+        b = res["batched_graph"]
+        out = {"metric": "batched TSQR problems/s (512 uneven FP32 problems)", "value": b["problems_per_s"],
+               "unit": "problems/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": b["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f32", "data": "synthetic: heights log-uniform [2048, 262144], widths {8,16,32,64}, "
+               "uniform[-1,1), seed 2024", "config": {"workload": "batched TSQR, 512 problems, one CUDA graph"},
+               "batched_graph": b, "loop_single": res["loop_single"], "rows": res["rows"],
+               "tflops": b["tflops"], "max_backward_sampled": res["max_backward_sampled"], "clocks": clocks}
+        if rank == 0:
+            print(json.dumps(out))
+        return 0
 
     A0 = make_input(m, n, 1234 + rank, device)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)

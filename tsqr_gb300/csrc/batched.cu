@@ -111,19 +111,20 @@ struct ClassCfg {
     void (*apply)(const ApplyTable&, int, cudaStream_t);
 };
 
-template <int NMAX, int NT, int RPT, int MINB, int AMINB>
+template <int NMAX, int NT, int RPT, int MINB, int AMINB, int ANT = NT>
 struct Cls {
+    static constexpr int ARPT = NT * RPT / ANT;  // the apply CTA covers the same tile height
     static constexpr size_t kSmem = apply_smem_bytes<float, NMAX, NT * RPT>();
     static void factor(const FactorTable& t, int grid, cudaStream_t s) {
         batched_factor<NMAX, NT, RPT, MINB><<<grid, NT, 0, s>>>(t);
     }
     static void apply(const ApplyTable& t, int grid, cudaStream_t s) {
         static bool attr = [] {
-            return cudaFuncSetAttribute(batched_apply<NMAX, NT, RPT, AMINB>,
+            return cudaFuncSetAttribute(batched_apply<NMAX, ANT, ARPT, AMINB>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem) == cudaSuccess;
         }();
         (void)attr;
-        batched_apply<NMAX, NT, RPT, AMINB><<<grid, NT, kSmem, s>>>(t);
+        batched_apply<NMAX, ANT, ARPT, AMINB><<<grid, ANT, kSmem, s>>>(t);
     }
     static ClassCfg cfg() { return {NMAX, NT * RPT, NT, kSmem, &factor, &apply}; }
 };
@@ -131,8 +132,8 @@ struct Cls {
 const ClassCfg& class_of(int n) {
     static const ClassCfg c8 = Cls<8, 256, 4, 3, 3>::cfg();
     static const ClassCfg c16 = Cls<16, 256, 2, 2, 3>::cfg();
-    static const ClassCfg c32 = Cls<32, 128, 4, 2, 2>::cfg();
-    static const ClassCfg c64 = Cls<64, 256, 1, 1, 1>::cfg();
+    static const ClassCfg c32 = Cls<32, 128, 4, 2, 2, 256>::cfg();
+    static const ClassCfg c64 = Cls<64, 128, 2, 2, 1, 256>::cfg();
     if (n <= 8) return c8;
     if (n <= 16) return c16;
     if (n <= 32) return c32;
@@ -169,8 +170,7 @@ int resident_grid(const ClassCfg& c, bool apply, int64_t tiles) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 148;
     }
-    (void)apply;
-    const int per_sm = c.nmax >= 64 ? 1 : 2;
+    const int per_sm = (apply && c.nmax >= 64) ? 1 : 2;  // resident CTAs per SM of each configuration
     return (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * per_sm));
 }
 

@@ -65,7 +65,7 @@ KernelSet<float> pick(float*, int n) {
     if (n <= 8) return make_set<TileCfg<float, 8, 256, 4, 3, 3>, float>();
     if (n <= 16) return make_set<TileCfg<float, 16, 256, 2, 2, 3>, float>();
     if (n <= 32) return make_set<TileCfg<float, 32, 128, 4, 2, 2, 256>, float>();
-    if (n <= 64) return make_set<TileCfg<float, 64, 256, 1, 1, 1>, float>();
+    if (n <= 64) return make_set<TileCfg<float, 64, 128, 2, 2, 1, 256>, float>();
     return KernelSet<float>();
 }
 KernelSet<double> pick(double*, int n) {
@@ -160,10 +160,9 @@ tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ld
 
 // ---------------------------------------------------------------------------
 // Precision form (FP32 entry points): the tile factorisation stays FP32 on
-// CUDA cores with the per-column norm, beta and tau in FP64; the root of the
-// tree (the stacked R factors of the last level, at most one tile) is
-// factored in FP64 by the double-precision tree and converted back; every
-// Q assembly of the down-sweep runs on tcgen05 in TF32x3 (tc_apply.cu).
+// CUDA cores; every Q assembly of the down-sweep runs on tcgen05 in TF32x3
+// (tc_apply.cu).  An FP64 root combine (the last level converted to double
+// and factored by the FP64 tree) is built in but switched off (kRoot64).
 // Workspace: [status word (256 B) | level matrices | FP64 root copy | FP64
 // root-tree workspace].
 // ---------------------------------------------------------------------------
@@ -204,7 +203,7 @@ PrecCfg pick_precision(int n) {
         c.ks = make_set<TileCfg<float, 32, 128, 4, 2, 2, 256>, float>();
     } else if (n <= 64) {
         c.nmax = 64;
-        c.ks = make_set<TileCfg<float, 64, 256, 1, 1, 1, 256>, float>();
+        c.ks = make_set<TileCfg<float, 64, 128, 2, 2, 1, 256>, float>();
     }
     c.rows = c.ks.rows;
     return c;
