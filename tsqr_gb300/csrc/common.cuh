@@ -78,14 +78,24 @@ __device__ __forceinline__ void warp_reduce_to_smem_x(float (&p)[NV], float* row
     for (int half = 0; half < (NV + 31) / 32; ++half) {
         const int idx = lane + 32 * half;
         if (idx < NV) {
-            float a = 0.f;
+            // pairwise (tree) sum: depth 5 instead of a 31-add chain
+            float a[32];
 #pragma unroll
-            for (int r = 0; r < 32; ++r) a += scratch[r * SP + idx];
-            row[idx] = a;
+            for (int r = 0; r < 32; ++r) a[r] = scratch[r * SP + idx];
+#pragma unroll
+            for (int w = 16; w >= 1; w >>= 1)
+#pragma unroll
+                for (int r = 0; r < w; ++r) a[r] += a[r + w];
+            row[idx] = a[0];
         }
     }
     __syncwarp();
 }
+
+// 1/x rounded to nearest (FP32: one reciprocal instruction sequence instead
+// of the general division routine).
+__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double recip(double x) { return 1.0 / x; }
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 __host__ __device__ inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }

@@ -29,21 +29,26 @@ namespace {
 
 template <int NMAX>
 struct TcApplySmem {
-    uint32_t a_hi[128 * NMAX];     // K-major A operand, one 128-row block
-    uint32_t a_lo[128 * NMAX];
     uint32_t b_hi[NMAX * NMAX];    // K-major B operand: W (K = NMAX rows of W, N = NMAX)
     uint32_t b_lo[NMAX * NMAX];
-    float Ws[NMAX][NMAX];
-    float Vt[NMAX][NMAX + 1];
-    float Tt[NMAX][NMAX + 1];
-    float Bs[NMAX][NMAX + 1];
-    float Ys[NMAX][NMAX + 1];
+    float Vt[NMAX][NMAX + 1];      // masked top block of V (read again by block 0)
+    float Bs[NMAX][NMAX + 1];      // the parent block B (read again by the epilogue)
+    union {
+        struct {                   // K-major A operand, one 128-row block
+            uint32_t a_hi[128 * NMAX];
+            uint32_t a_lo[128 * NMAX];
+        } op;
+        struct {                   // scratch of the W products, dead before staging starts
+            float Tt[NMAX][NMAX + 1];
+            float Ys[NMAX][NMAX + 1];
+        } w;
+    } u;
     unsigned long long mbar;
     uint32_t tmem_slot;
 };
 
 template <int NMAX, int B>
-__global__ void __launch_bounds__(128) tc_apply_tiles(ApplyParams<float> p, int* err) {
+__global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyParams<float> p, int* err) {
     static_assert(NMAX % 16 == 0 && NMAX <= 256 && B % 128 == 0, "bad shape");
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     TcApplySmem<NMAX>& S = *reinterpret_cast<TcApplySmem<NMAX>*>(tc_smem_raw);
@@ -77,7 +82,7 @@ __global__ void __launch_bounds__(128) tc_apply_tiles(ApplyParams<float> p, int*
             const bool in = (r < ht && r < n && c < n);
             const float v = in ? tile[r + c * p.ld] : 0.f;
             S.Vt[r][c] = (r > c) ? v : ((r == c && c < n) ? 1.f : 0.f);
-            S.Tt[r][c] = (r <= c) ? v : 0.f;
+            S.u.w.Tt[r][c] = (r <= c) ? v : 0.f;
             float b;
             if (p.P)
                 b = (r < n && c < n) ? p.P[t * n + r + c * p.ldp] : 0.f;
@@ -86,26 +91,43 @@ __global__ void __launch_bounds__(128) tc_apply_tiles(ApplyParams<float> p, int*
             S.Bs[r][c] = b;
         }
         __syncthreads();
-        for (int idx = tid; idx < NMAX * NMAX; idx += 128) {
-            const int k = idx % NMAX, c = idx / NMAX;
-            float a = 0;
+        // Each thread owns output row k and CPT columns c0 + CS*j: CPT
+        // independent accumulators per pass instead of serial dot chains.
+        constexpr int CPT = NMAX * NMAX / 128, CS = 128 / NMAX;
+        const int k = tid % NMAX, c0 = tid / NMAX;
+        {
+            float acc[CPT];
 #pragma unroll
-            for (int r = 0; r < NMAX; ++r) a += S.Vt[r][k] * S.Bs[r][c];
-            S.Ys[k][c] = a;
+            for (int j = 0; j < CPT; ++j) acc[j] = 0.f;
+#pragma unroll
+            for (int r = 0; r < NMAX; ++r) {
+                const float vk = S.Vt[r][k];
+#pragma unroll
+                for (int j = 0; j < CPT; ++j) acc[j] += vk * S.Bs[r][c0 + CS * j];
+            }
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) S.u.w.Ys[k][c0 + CS * j] = acc[j];  // Y = V_top^T B
         }
         __syncthreads();
-        for (int idx = tid; idx < NMAX * NMAX; idx += 128) {
-            const int k = idx % NMAX, c = idx / NMAX;
-            float a = 0;
+        {
+            float acc[CPT];
 #pragma unroll
-            for (int l = 0; l < NMAX; ++l) a += S.Tt[k][l] * S.Ys[l][c];
-            S.Ws[k][c] = a;
-            // B operand element (row = output column c, K index k)
-            uint32_t hi, lo;
-            tc::split_tf32(a, hi, lo);
-            const uint32_t off = tc::kmajor_off(c, k, NMAX) >> 2;
-            S.b_hi[off] = hi;
-            S.b_lo[off] = lo;
+            for (int j = 0; j < CPT; ++j) acc[j] = 0.f;
+#pragma unroll
+            for (int l = 0; l < NMAX; ++l) {
+                const float tkl = S.u.w.Tt[k][l];
+#pragma unroll
+                for (int j = 0; j < CPT; ++j) acc[j] += tkl * S.u.w.Ys[l][c0 + CS * j];
+            }
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) {
+                // W = T Y as the B operand (row = output column c, K index k)
+                uint32_t hi, lo;
+                tc::split_tf32(acc[j], hi, lo);
+                const uint32_t off = tc::kmajor_off(c0 + CS * j, k, NMAX) >> 2;
+                S.b_hi[off] = hi;
+                S.b_lo[off] = lo;
+            }
         }
 
         // --- blocks of 128 rows ------------------------------------------
@@ -138,15 +160,15 @@ __global__ void __launch_bounds__(128) tc_apply_tiles(ApplyParams<float> p, int*
                 tc::split_tf32(v[k4 + 2], hi.z, lo.z);
                 tc::split_tf32(v[k4 + 3], hi.w, lo.w);
                 const uint32_t off = tc::kmajor_off(tid, k4, NMAX);
-                *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(S.a_hi) + off) = hi;
-                *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(S.a_lo) + off) = lo;
+                *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(S.u.op.a_hi) + off) = hi;
+                *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(S.u.op.a_lo) + off) = lo;
             }
             tc::fence_smem_to_async();
             tc::fence_before_sync();
             __syncthreads();
             if (tid == 0) {
                 tc::fence_after_sync();
-                const uint32_t ah = tc::smem_u32(S.a_hi), al = tc::smem_u32(S.a_lo);
+                const uint32_t ah = tc::smem_u32(S.u.op.a_hi), al = tc::smem_u32(S.u.op.a_lo);
                 const uint32_t bh = tc::smem_u32(S.b_hi), bl = tc::smem_u32(S.b_lo);
 #pragma unroll
                 for (int ks = 0; ks < NMAX / 8; ++ks) {

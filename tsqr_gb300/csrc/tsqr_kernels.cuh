@@ -157,8 +157,10 @@ __device__ __forceinline__ void factor_tile(FactorSmem<T, NMAX, NT, NORM64>& S, 
                     } else {
                         const N64 nrm = sqrt(alpha * alpha + sigma2);
                         beta = (alpha >= N64(0)) ? -nrm : nrm;
-                        tau = (beta - alpha) / beta;
-                        scale = N64(1) / (alpha - beta);
+                        // reciprocal-multiply (round-to-nearest reciprocal)
+                        // keeps the slow division path off the column chain
+                        tau = (beta - alpha) * recip(beta);
+                        scale = recip(alpha - beta);
                     }
                     const T taut = (T)tau;
                     const T scalet = (T)scale;
