@@ -71,6 +71,21 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
     uint32_t phase = 0;
     bool ok = true;
 
+    // Row `blk*128 + tid` of tile tt into v (zero past the tile; the top
+    // n rows come masked from Vt instead).  Issued one block ahead, and for
+    // the first block of the next tile before this tile's W products, so
+    // the global loads are in flight while the CTA computes.
+    float vnext[NMAX];
+    auto load_block = [&](int64_t tt, int blk, float(&v)[NMAX]) {
+        const int64_t r0 = tt * B;
+        const int htt = (int)((p.h - r0) < B ? (p.h - r0) : B);
+        const float* tl = p.M + r0;
+        const int r = blk * 128 + tid;
+#pragma unroll
+        for (int k = 0; k < NMAX; ++k) v[k] = (r >= n && r < htt && k < n) ? tl[r + (int64_t)k * p.ld] : 0.f;
+    };
+    if (blockIdx.x < p.ntiles) load_block(blockIdx.x, 0, vnext);
+
     for (int64_t t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
         const int64_t row0 = t * B;
         const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
@@ -131,21 +146,7 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
         }
 
         // --- blocks of 128 rows ------------------------------------------
-        float vnext[NMAX];
-        auto load_row = [&](int blk, float (&v)[NMAX]) {
-            const int r = blk * 128 + tid;
-#pragma unroll
-            for (int k = 0; k < NMAX; ++k) {
-                float x;
-                if (r < n)
-                    x = 0.f;  // top-block rows come masked from Vt below
-                else
-                    x = (r < ht && k < n) ? tile[r + (int64_t)k * p.ld] : 0.f;
-                v[k] = x;
-            }
-        };
         const int nblk = (ht + 127) / 128;
-        load_row(0, vnext);
         __syncthreads();  // Vt complete (masked top rows)
         for (int blk = 0; blk < nblk; ++blk) {
             const int r = blk * 128 + tid;
@@ -182,7 +183,10 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
                 tc::mma_commit(mbar);
             }
             // prefetch the next block's rows while the tensor core works
-            if (blk + 1 < nblk) load_row(blk + 1, vnext);
+            if (blk + 1 < nblk)
+                load_block(t, blk + 1, vnext);
+            else if (t + gridDim.x < p.ntiles)
+                load_block(t + gridDim.x, 0, vnext);
             const bool waited = tc::mbar_wait(mbar, phase);
             // a timed-out wait anywhere stops the whole CTA (uniform decision)
             if (__syncthreads_or(!waited)) {
@@ -236,11 +240,17 @@ void launch(const ApplyParams<float>& p, int grid, int* err, cudaStream_t s) {
 
 // Tile heights must match the factor configuration of the precision path.
 bool tc_apply_level(const ApplyParams<float>& p, int nmax, int rows, int* err, cudaStream_t s) {
-    const int grid = (int)(p.ntiles < 1 ? 1 : (p.ntiles > (1 << 30) ? (1 << 30) : p.ntiles));
+    // persistent grid: resident CTAs walk the tiles, prefetching the next one
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 148;
+    }
+    const int64_t resident = (int64_t)sms * (nmax <= 32 ? 4 : 1);
+    const int grid = (int)(p.ntiles < 1 ? 1 : (p.ntiles > resident ? resident : p.ntiles));
     if (nmax == 32 && rows == 512) {
         launch<32, 512>(p, grid, err, s);
-    } else if (nmax == 64 && rows == 256) {
-        launch<64, 256>(p, grid, err, s);
     } else {
         return false;
     }

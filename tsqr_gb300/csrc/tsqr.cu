@@ -295,9 +295,20 @@ tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R
         ap.ntiles = lv[l].ntiles;
         ap.P = (l == L - 1) ? nullptr : lv[l + 1].M;
         ap.ldp = (l == L - 1) ? 0 : lv[l + 1].ld;
-        ap.vec = 0;
-        if (!tc_apply_level(ap, c.nmax, c.rows, err, s)) return TSQR_ERR_UNSUPPORTED;
-        log_launch(kTagTc + l, s);
+        if (c.nmax <= 32) {
+            ap.vec = 0;
+            if (!tc_apply_level(ap, c.nmax, c.rows, err, s)) return TSQR_ERR_UNSUPPORTED;
+            log_launch(kTagTc + l, s);
+        } else {
+            // 32 < n <= 64: the per-tile W = T (V_top^T B) setup is O(n^3) on
+            // CUDA cores for every 256-row tile and outweighs what the tensor
+            // cores save on V W (measured 7.0 ms vs 4.0 ms for the level-0
+            // apply at 4,194,304 x 64), so the CUDA-core apply runs instead.
+            constexpr int ve = 4;
+            ap.vec = (lv[l].ld % ve == 0 && (reinterpret_cast<uintptr_t>(lv[l].M) % 16) == 0) ? 1 : 0;
+            c.ks.apply(ap, (int)std::min<int64_t>(lv[l].ntiles, 1 << 30), s);
+            log_launch(kTagApply + l, s);
+        }
     }
     return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
 }
