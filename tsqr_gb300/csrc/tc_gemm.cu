@@ -45,7 +45,8 @@ struct GemmSmem {
 
 template <bool TRANS_A, int NB>
 __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, const float* __restrict__ A, int64_t lda,
-                                                      const float* __restrict__ Bm, int64_t ldb, float* C, int64_t ldc,
+                                                      const float* __restrict__ Bm, int64_t ldb, float* __restrict__ C,
+                                                      int64_t ldc,
                                                       float alpha, int64_t kchunk, int* err) {
     extern __shared__ __align__(1024) unsigned char gemm_smem_raw[];
     GemmSmem<NB>& S = *reinterpret_cast<GemmSmem<NB>*>(gemm_smem_raw);
@@ -194,21 +195,30 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
         const int m = m0 + 32 * warp + (tid & 31);
         float* Cz = TRANS_A ? C + (int64_t)blockIdx.z * M * N : C;
         const int64_t ldz = TRANS_A ? M : ldc;
-#pragma unroll 1
+#pragma unroll 2
         for (int c8 = 0; c8 < NB; c8 += 8) {
             float d[8];
             tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c8, d);
             tc::tmem_ld_wait();
             if (m < M) {
+                if (TRANS_A) {
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const int nn = n0 + c8 + e;
-                    if (nn < N) {
-                        float* dst = Cz + m + (int64_t)nn * ldz;
-                        if (TRANS_A)
-                            *dst = nstage > 0 ? d[e] : 0.f;
-                        else if (nstage > 0)
-                            *dst = *dst + alpha * d[e];
+                    for (int e = 0; e < 8; ++e) {
+                        const int nn = n0 + c8 + e;
+                        if (nn < N) Cz[m + (int64_t)nn * ldz] = nstage > 0 ? d[e] : 0.f;
+                    }
+                } else if (nstage > 0) {
+                    // all eight loads first, so their latencies overlap
+                    float c[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const int nn = n0 + c8 + e;
+                        c[e] = (nn < N) ? Cz[m + (int64_t)nn * ldz] : 0.f;
+                    }
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const int nn = n0 + c8 + e;
+                        if (nn < N) Cz[m + (int64_t)nn * ldz] = c[e] + alpha * d[e];
                     }
                 }
             }
