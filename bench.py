@@ -117,14 +117,27 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def orthonormal_columns(G):
+    """Orthonormal basis of G's columns by two CholeskyQR passes in FP64: the
+    n x n Cholesky factor and its inverse on the host, the m x n product on
+    the device.  Avoids the device QR of torch (a separately loaded library
+    that is not present under every profiler)."""
+    import torch
+    for _ in range(2):
+        C = (G.t() @ G).cpu()
+        Linv = torch.linalg.inv(torch.linalg.cholesky(C))
+        G = G @ Linv.t().to(G.device)
+    return G
+
+
 def make_input(m, n, seed, device):
     """A = U diag(sigma) V^T, sigma geometric 1 -> 1e-6 (condition 1e6)."""
     import torch
     g = torch.Generator(device=device).manual_seed(seed)
     G = torch.randn((m, n), generator=g, device=device, dtype=torch.float64)
-    U, _ = torch.linalg.qr(G)
+    U = orthonormal_columns(G)
     H = torch.randn((n, n), generator=g, device=device, dtype=torch.float64)
-    V, _ = torch.linalg.qr(H)
+    V = orthonormal_columns(H)
     sig = torch.logspace(0, -6, n, device=device, dtype=torch.float64)
     A = (U * sig) @ V.t()
     del G, U

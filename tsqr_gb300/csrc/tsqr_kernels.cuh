@@ -65,6 +65,14 @@ struct ApplyParams {
     int vec;        // 1: ld and the level base allow 16-byte copies
 };
 
+// Column-major V^T V of a tile: Sc[j][k] = S(k, j) = v_k . v_j for k < j,
+// rows padded to a multiple of 16 bytes so a column reads as vector loads.
+template <typename T, int NMAX>
+struct SCols {
+    static constexpr int LD = NMAX + 16 / (int)sizeof(T);
+    __align__(16) T c[NMAX][LD];
+};
+
 // Shared memory of one factor CTA.
 template <typename T, int NMAX, int NT, bool NORM64>
 struct FactorSmem {
@@ -74,7 +82,7 @@ struct FactorSmem {
     T s_alpha;
     T red[NW][NMAX];
     __align__(16) T wfin[NW][NMAX];
-    T Ssh[NMAX][NMAX + 1];
+    SCols<T, NMAX> Sc;
     T Tsh[NMAX][NMAX + 1];
     T tau_sh[NMAX];
     T rdiag[NMAX];
@@ -82,6 +90,38 @@ struct FactorSmem {
     __align__(16) float xpose[std::is_same<T, float>::value ? NW : 1]
                              [std::is_same<T, float>::value ? 32 * xpose_stride<NMAX>() : 4];
 };
+
+// Row i of the compact-WY factor T of a tile: T(i,i) = tau_i and
+// T(i,j) = -tau_j sum_{k=i}^{j-1} T(i,k) S(k,j) for i < j < n, zero
+// elsewhere.  Column j of S is read with 16-byte loads that do not depend on
+// the FMA chain, so their latency is paid once per column instead of once per
+// product, and the chain is split into two accumulators.  T(i,k) = 0 for
+// k < i, so the sum runs over every k < j without a per-thread test.
+template <typename T, int NMAX>
+__device__ __forceinline__ void t_factor_row(const SCols<T, NMAX>& S, const T* tau, int i, int n, T (&trow)[NMAX]) {
+    constexpr int VW = 16 / (int)sizeof(T);  // elements per 16-byte load
+    static_assert(NMAX % VW == 0, "T build reads whole 16-byte groups");
+#pragma unroll
+    for (int j = 0; j < NMAX; ++j) {
+        T a0 = T(0), a1 = T(0);
+#pragma unroll
+        for (int k0 = 0; k0 < j; k0 += VW) {
+            if constexpr (VW == 4) {
+                const float4 q = *reinterpret_cast<const float4*>(&S.c[j][k0]);
+                a0 += trow[k0] * q.x;
+                if (k0 + 1 < j) a1 += trow[k0 + 1] * q.y;
+                if (k0 + 2 < j) a0 += trow[k0 + 2] * q.z;
+                if (k0 + 3 < j) a1 += trow[k0 + 3] * q.w;
+            } else {
+                const double2 q = *reinterpret_cast<const double2*>(&S.c[j][k0]);
+                a0 += trow[k0] * q.x;
+                if (k0 + 1 < j) a1 += trow[k0 + 1] * q.y;
+            }
+        }
+        const T tj = tau[j];
+        trow[j] = (j == i) ? tj : ((j > i && j < n) ? -tj * (a0 + a1) : T(0));
+    }
+}
 
 // Householder QR of one tile: ht (<= NT*RPT) rows of n columns at `tile`
 // (leading dimension ld), factored in place (V below the diagonal, T in the
@@ -98,7 +138,7 @@ __device__ __forceinline__ void factor_tile(FactorSmem<T, NMAX, NT, NORM64>& S, 
     auto& s_alpha = S.s_alpha;
     auto& red = S.red;
     auto& wfin = S.wfin;
-    auto& Ssh = S.Ssh;
+    auto& Sc = S.Sc.c;
     auto& Tsh = S.Tsh;
     auto& tau_sh = S.tau_sh;
     auto& rdiag = S.rdiag;
@@ -204,7 +244,7 @@ __device__ __forceinline__ void factor_tile(FactorSmem<T, NMAX, NT, NORM64>& S, 
                                 wfin[warp][idx] = (idx > u && idx < live) ? a : T(0);
                                 if (warp == 0) {
                                     const int k = (idx >= past0) ? idx - past0 : ((idx < u) ? base + idx : -1);
-                                    if (k >= 0) Ssh[k][j] = a;
+                                    if (k >= 0) Sc[j][k] = a;
                                 }
                             }
                         }
@@ -239,27 +279,14 @@ __device__ __forceinline__ void factor_tile(FactorSmem<T, NMAX, NT, NORM64>& S, 
                 for (int u = 0; u < U; ++u) y[i][NMAX - U + u] = keep[u];
             }
         }
-        __syncthreads();  // Ssh, tau_sh, rdiag complete
+        __syncthreads();  // V^T V, tau_sh, rdiag complete
 
         // T, one row per thread: T(i,i) = tau_i,
         // T(i,j) = -tau_j sum_{k=i}^{j-1} T(i,k) S(k,j) for j > i.
         if (tid < n) {
             const int i = tid;
             T trow[NMAX];
-#pragma unroll
-            for (int j = 0; j < NMAX; ++j) {
-                T val = T(0);
-                if (j == i) {
-                    val = tau_sh[j];
-                } else if (j > i && j < n) {
-                    T a = 0;
-#pragma unroll
-                    for (int k = 0; k < j; ++k)
-                        if (k >= i) a += trow[k] * Ssh[k][j];
-                    val = -tau_sh[j] * a;
-                }
-                trow[j] = val;
-            }
+            t_factor_row<T, NMAX>(S.Sc, tau_sh, i, n, trow);
 #pragma unroll
             for (int j = 0; j < NMAX; ++j) Tsh[i][j] = trow[j];
         }
@@ -302,6 +329,501 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
         const int64_t row0 = t * B;
         const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
         factor_tile<T, NMAX, NT, RPT, NORM64>(S, p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n, p.ldr);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Warp tiles (FP32, n <= 32).  One warp factors a tile of 32*RPT rows by
+// itself: row lane + 32*i sits in register row y[i].  Every reduction is a
+// warp shuffle or a per-warp shared-memory transpose, so there is no block
+// barrier on the column chain, and the warps of a CTA (and of an SM) work on
+// independent tiles: the per-column latency (norm -> reflector -> dots ->
+// update) is hidden by the other tiles in flight instead of being paid once
+// per 512-row tile under block barriers.  Same arithmetic and output format
+// as factor_tile (V in place, T in the top block's upper triangle, R to the
+// next level), only the tile is shorter, so the tree has more levels.
+template <int NMAX>
+struct WarpFactorSmem {
+    __align__(16) float xpose[32 * xpose_stride<NMAX>()];  // transpose scratch of the dot products
+    __align__(16) float coef[NMAX];                         // update coefficients (0 off the trailing columns)
+    SCols<float, NMAX> Sc;                                  // V^T V (strict upper part, by column)
+    float tau[NMAX];
+    float rdiag[NMAX];
+};
+
+template <int NMAX, int RPT, int U = 4>
+__device__ __forceinline__ void factor_warp_tile(WarpFactorSmem<NMAX>& S, float* tile, int64_t ld, int ht, int n,
+                                                 float* Rt, int64_t ldr) {
+    constexpr int SP = xpose_stride<NMAX>();
+    static_assert(NMAX <= 32 && NMAX % U == 0, "warp tiles hold at most 32 columns");
+    const int lane = threadIdx.x & 31;
+    const int G = (n + U - 1) / U;
+    const int shift = (U * G) % NMAX;
+    // Register layout and rotation as in factor_tile: at group g position
+    // c < n - U*g holds column U*g + c, position NMAX - U*g + k holds v_k.
+    float y[RPT][NMAX];
+#pragma unroll
+    for (int i = 0; i < RPT; ++i) {
+        const int r = lane + 32 * i;
+#pragma unroll
+        for (int c = 0; c < NMAX; ++c) y[i][c] = (r < ht && c < n) ? tile[r + c * ld] : 0.f;
+    }
+    float* mine = S.xpose + lane * SP;
+
+    // Look-ahead: the norm of column j+1 is reduced (shuffles, square root,
+    // reciprocals) while the rest of step j's update is still being issued,
+    // so the next column's reflector is ready when the update ends.  Every
+    // group runs all U steps without a branch; steps past column n-1 work on
+    // zero columns (tau = 0, coefficient 0) and change nothing that is kept.
+    float sig2, alpha;
+    {
+        float s = 0.f;
+#pragma unroll
+        for (int i = 0; i < RPT; ++i)
+            if (i > 0 || lane > 0) s = fmaf(y[i][0], y[i][0], s);
+        alpha = __shfl_sync(kFull, y[0][0], 0);
+        sig2 = warp_sum(s);
+    }
+
+#pragma unroll 1
+    for (int g = 0; g < G; ++g) {
+        const int base = U * g;
+        const int live = n - base;
+        const int past0 = NMAX - base;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = base + u;
+            // (a) reflector of column j from sigma^2 = ||x(j+1:, j)||^2 and
+            // alpha = x(j, j).  The xor butterfly leaves the bitwise same sum
+            // in every lane, so beta, tau and the scale agree across the warp.
+            const bool zero = (sig2 == 0.f);
+            const float nrm = sqrtf(fmaf(alpha, alpha, sig2));
+            const float beta = zero ? alpha : ((alpha >= 0.f) ? -nrm : nrm);
+            const float tau = zero ? 0.f : (beta - alpha) * recip(beta);
+            const float scale = zero ? 0.f : recip(alpha - beta);
+            // (b) v_j (v_j(j) = 1, 0 above the diagonal)
+#pragma unroll
+            for (int i = 0; i < RPT; ++i)
+                if (i > 0 || lane > j) y[i][u] *= scale;
+            const float v0 = (lane > j) ? y[0][u] : ((lane == j) ? 1.f : 0.f);
+            // (c) partial dots v_j . y[c] of every other position, four at a
+            // time into this lane's transpose row
+#pragma unroll
+            for (int c4 = 0; c4 < NMAX; c4 += 4) {
+                float q[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int c = c4 + e;
+                    q[e] = (c != u) ? v0 * y[0][c] : 0.f;
+#pragma unroll
+                    for (int i = 1; i < RPT; ++i)
+                        if (c != u) q[e] = fmaf(y[i][u], y[i][c], q[e]);
+                }
+                *reinterpret_cast<float4*>(mine + c4) = make_float4(q[0], q[1], q[2], q[3]);
+            }
+            __syncwarp();
+            // (d) lane c sums position c over the warp (pairwise, in four
+            // groups of eight rows), then publishes the update coefficient
+            // and, for finished reflectors, column j of V^T V
+            if (lane < NMAX) {
+                float part[4];
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    float a[8];
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) a[r] = S.xpose[(8 * h + r) * SP + lane];
+#pragma unroll
+                    for (int w = 4; w >= 1; w >>= 1)
+#pragma unroll
+                        for (int r = 0; r < w; ++r) a[r] += a[r + w];
+                    part[h] = a[0];
+                }
+                const float d = (part[0] + part[1]) + (part[2] + part[3]);
+                S.coef[lane] = (lane > u && lane < live) ? d : 0.f;
+                const int k = (lane >= past0) ? lane - past0 : ((lane < u) ? base + lane : -1);
+                if (k >= 0) S.Sc.c[j][k] = d;
+            }
+            if (lane == 0) {
+                S.tau[j] = tau;
+                S.rdiag[j] = beta;
+            }
+            __syncwarp();
+            // (e) x_c -= tau (v^T x_c) v on the positions after u: position
+            // u+1 first, then its norm is started, then the rest
+            float tv[RPT];
+            tv[0] = tau * v0;
+#pragma unroll
+            for (int i = 1; i < RPT; ++i) tv[i] = tau * y[i][u];
+            float cf[NMAX];
+#pragma unroll
+            for (int c4 = 0; c4 < NMAX; c4 += 4) {
+                if (c4 + 3 <= u) continue;
+                const float4 w4 = *reinterpret_cast<const float4*>(S.coef + c4);
+                cf[c4] = w4.x;
+                cf[c4 + 1] = w4.y;
+                cf[c4 + 2] = w4.z;
+                cf[c4 + 3] = w4.w;
+            }
+            if (u + 1 < NMAX) {
+                const int c = (u + 1 < NMAX) ? u + 1 : 0;  // keeps the index in range when u + 1 == NMAX
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) y[i][c] = fmaf(-tv[i], cf[c], y[i][c]);
+                float s = 0.f;
+#pragma unroll
+                for (int i = 0; i < RPT; ++i)
+                    if (i > 0 || lane > j + 1) s = fmaf(y[i][c], y[i][c], s);
+                alpha = __shfl_sync(kFull, y[0][c], (j + 1) & 31);
+                sig2 = warp_sum(s);
+            }
+#pragma unroll
+            for (int c = u + 2; c < NMAX; ++c)
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) y[i][c] = fmaf(-tv[i], cf[c], y[i][c]);
+        }
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+            float keep[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) keep[u] = y[i][u];
+#pragma unroll
+            for (int c = 0; c < NMAX - U; ++c) y[i][c] = y[i][c + U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) y[i][NMAX - U + u] = keep[u];
+        }
+    }
+    __syncwarp();  // tau, rdiag and V^T V of the last column are visible
+
+    // R (row r < n is lane r's slot 0) and V below the diagonal.
+    if (lane < n) {
+#pragma unroll
+        for (int c = 0; c < NMAX; ++c) {
+            const int k = (c + shift) % NMAX;
+            if (k < n) {
+                float v = (k > lane) ? y[0][c] : ((k == lane) ? S.rdiag[lane] : 0.f);
+                if (lane >= ht) v = 0.f;
+                Rt[lane + k * ldr] = v;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < RPT; ++i) {
+        const int r = lane + 32 * i;
+        if (r < ht) {
+#pragma unroll
+            for (int c = 0; c < NMAX; ++c) {
+                const int k = (c + shift) % NMAX;
+                if (k < n && r > k) tile[r + k * ld] = y[i][c];
+            }
+        }
+    }
+    // T in the top block's upper triangle (diagonal included), row i by lane
+    // i: T(i,i) = tau_i, T(i,j) = -tau_j sum_{k=i}^{j-1} T(i,k) S(k,j).
+    if (lane < n && lane < ht) {
+        const int i = lane;
+        float trow[NMAX];
+        t_factor_row<float, NMAX>(S.Sc, S.tau, i, n, trow);
+#pragma unroll
+        for (int j = 0; j < NMAX; ++j)
+            if (j >= i && j < n) tile[i + j * ld] = trow[j];
+    }
+    __syncwarp();  // the next tile of this warp reuses S
+}
+
+template <int NMAX, int RPT, int WPB, int MINB, int U = 4>
+__global__ void __launch_bounds__(32 * WPB, MINB) factor_warp_tiles(FactorParams<float> p) {
+    constexpr int B = 32 * RPT;
+    __shared__ WarpFactorSmem<NMAX> S[WPB];
+    const int warp = threadIdx.x >> 5;
+    for (int64_t t = (int64_t)blockIdx.x * WPB + warp; t < p.ntiles; t += (int64_t)gridDim.x * WPB) {
+        const int64_t row0 = t * B;
+        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
+        factor_warp_tile<NMAX, RPT, U>(S[warp], p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n, p.ldr);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Column-split tiles (FP32, n <= NMAX <= 32, tiles of 32*RPT rows).  The W = NMAX/CW
+// warps of a CTA share one tile: warp w holds columns [w*CW, w*CW + CW) of
+// all 32*RPT rows (row lane + 32*i in y[i]), so a thread carries RPT*CW
+// tile values instead of RPT*NMAX.  Column j
+// is owned by warp j/CW.  At step j the owner forms v_j and tau_j from its
+// column, publishes them to shared memory and passes one CTA barrier; then
+// every warp applies H_j to its own columns (dot products, a per-warp
+// transpose reduction, the rank-1 update) while the owner goes on to column
+// j+1.  Warps whose columns are all finished only take the dot products that
+// give column j of V^T V.  The critical path of a step is the owner's chain
+// for one CW-column block instead of the whole tile.  v_j alternates between
+// two buffers: the owner rewrites buffer b at step j+2, after every warp has
+// passed the barrier of step j+1 and so has read step j's copy.
+//
+// Every warp executes the same number of barriers (one per step; a phase of
+// nloc columns runs 4*ceil(nloc/4) steps, the padding steps act on zero
+// columns with tau = 0).  Output format as factor_tile.
+// Row stride of the per-warp transpose scratch: CW = 4 needs no padding
+// (lane l's 16-byte row is words 4l..4l+3, and the column reads of the 8
+// lanes per position hit 32 distinct banks); wider rows get 4 words of pad.
+template <int CW>
+__host__ __device__ constexpr int colsum_stride() {
+    return CW == 4 ? 4 : CW + 4;
+}
+
+template <int NMAX, int CW, int RPT>
+struct SplitFactorSmem {
+    static constexpr int W = NMAX / CW;
+    __align__(16) float vbuf[2][32 * RPT];
+    float taub[2];
+    __align__(16) float xpose[W][32 * colsum_stride<CW>()];
+    __align__(16) float coef[W][CW];
+    SCols<float, NMAX> Sc;
+    float tau[NMAX];
+    float rdiag[NMAX];
+};
+
+// CTA barrier 1 over `count` threads; non-aligned form, since the owner and
+// the other warps reach it from different code.
+__device__ __forceinline__ void step_barrier(int count) {
+    asm volatile("barrier.sync 1, %0;\n" ::"r"(count) : "memory");
+}
+
+// Sum CW per-lane partials over the warp through a shared-memory transpose:
+// returns, in lane l, the full sum of position l % CW (32/CW lanes hold each
+// sum, bitwise equal).
+template <int CW>
+__device__ __forceinline__ float warp_colsum(const float (&q)[CW], float* scratch, int lane) {
+    constexpr int SP = colsum_stride<CW>();
+    constexpr int LPP = 32 / CW;  // lanes per position
+    constexpr int RPL = 32 / LPP;  // rows summed by one lane
+    float* mine = scratch + lane * SP;
+#pragma unroll
+    for (int c = 0; c < CW; c += 4) *reinterpret_cast<float4*>(mine + c) = make_float4(q[c], q[c + 1], q[c + 2], q[c + 3]);
+    __syncwarp();
+    const int p = lane % CW, h = lane / CW;
+    float a[RPL];
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) a[r] = scratch[(h + LPP * r) * SP + p];
+#pragma unroll
+    for (int w = RPL / 2; w >= 1; w >>= 1)
+#pragma unroll
+        for (int r = 0; r < w; ++r) a[r] += a[r + w];
+    float s = a[0];
+#pragma unroll
+    for (int o = CW; o < 32; o <<= 1) s += __shfl_xor_sync(kFull, s, o);
+    __syncwarp();  // scratch is rewritten by the next call
+    return s;
+}
+
+template <int NMAX, int CW, int RPT>
+__device__ __forceinline__ void factor_split_tile(SplitFactorSmem<NMAX, CW, RPT>& S, float* tile, int64_t ld, int ht,
+                                                  int n, float* Rt, int64_t ldr) {
+    constexpr int W = NMAX / CW;
+    constexpr int U = 4;
+    static_assert(NMAX <= 32 && CW % U == 0 && NMAX % CW == 0 && W >= 2, "bad split configuration");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int col0 = warp * CW;
+    const int mycols = max(0, min(CW, n - col0));
+    float* scratch = S.xpose[warp];
+
+    float y[RPT][CW];
+    {
+        // one column pointer stepped by ld; the row offsets 32*i are immediates
+        const float* pcol = tile + (int64_t)col0 * ld + lane;
+#pragma unroll
+        for (int c = 0; c < CW; ++c) {
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) y[i][c] = (lane + 32 * i < ht && c < mycols) ? pcol[32 * i] : 0.f;
+            pcol += ld;
+        }
+    }
+    int shift = 0;  // after this warp's own phase, position c holds its local column (c + shift) % CW
+
+#pragma unroll 1
+    for (int ph = 0; ph < W; ++ph) {
+        const int pc0 = ph * CW;
+        const int nloc = min(CW, n - pc0);
+        if (nloc <= 0) break;  // same for every warp
+        const int G = (nloc + U - 1) / U;
+        if (warp == ph) {
+            // ---- owner: reflectors of columns pc0 .. pc0+nloc-1, in groups of
+            // U with the register rotation of factor_tile, and the norm of the
+            // next column reduced while the current update is issued
+            float sig2, alpha;
+            {
+                float s = 0.f;
+#pragma unroll
+                for (int i = 0; i < RPT; ++i)
+                    if (i > 0 || lane > pc0) s = fmaf(y[i][0], y[i][0], s);
+                alpha = __shfl_sync(kFull, y[0][0], pc0 & 31);
+                sig2 = warp_sum(s);
+            }
+#pragma unroll 1
+            for (int g = 0; g < G; ++g) {
+                const int base = U * g;
+                const int live = nloc - base;
+                const int past0 = CW - base;
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int j = pc0 + base + u;
+                    const bool zero = (sig2 == 0.f);
+                    const float nrm = sqrtf(fmaf(alpha, alpha, sig2));
+                    const float beta = zero ? alpha : ((alpha >= 0.f) ? -nrm : nrm);
+                    const float tau = zero ? 0.f : (beta - alpha) * recip(beta);
+                    const float scale = zero ? 0.f : recip(alpha - beta);
+#pragma unroll
+                    for (int i = 0; i < RPT; ++i)
+                        if (i > 0 || lane > j) y[i][u] *= scale;
+                    const float v0 = (lane > j) ? y[0][u] : ((lane == j) ? 1.f : 0.f);
+                    const int b = j & 1;
+                    S.vbuf[b][lane] = v0;
+#pragma unroll
+                    for (int i = 1; i < RPT; ++i) S.vbuf[b][lane + 32 * i] = y[i][u];
+                    if (lane == 0) {
+                        S.taub[b] = tau;
+                        S.tau[j] = tau;
+                        S.rdiag[j] = beta;
+                    }
+                    step_barrier(W * 32);
+                    float q[CW];
+#pragma unroll
+                    for (int c = 0; c < CW; ++c) {
+                        q[c] = (c != u) ? v0 * y[0][c] : 0.f;
+#pragma unroll
+                        for (int i = 1; i < RPT; ++i)
+                            if (c != u) q[c] = fmaf(y[i][u], y[i][c], q[c]);
+                    }
+                    const float d = warp_colsum<CW>(q, scratch, lane);
+                    if (lane < CW) {
+                        S.coef[warp][lane] = (lane > u && lane < live) ? d : 0.f;
+                        const int k = (lane >= past0) ? lane - past0 : ((lane < u) ? base + lane : -1);
+                        if (k >= 0) S.Sc.c[j][pc0 + k] = d;
+                    }
+                    __syncwarp();
+                    float tv[RPT];
+                    tv[0] = tau * v0;
+#pragma unroll
+                    for (int i = 1; i < RPT; ++i) tv[i] = tau * y[i][u];
+                    float cf[CW];
+#pragma unroll
+                    for (int c4 = 0; c4 < CW; c4 += 4) {
+                        if (c4 + 3 <= u) continue;
+                        const float4 w4 = *reinterpret_cast<const float4*>(&S.coef[warp][c4]);
+                        cf[c4] = w4.x;
+                        cf[c4 + 1] = w4.y;
+                        cf[c4 + 2] = w4.z;
+                        cf[c4 + 3] = w4.w;
+                    }
+                    if (u + 1 < CW) {
+                        const int c = (u + 1 < CW) ? u + 1 : 0;  // keeps the index in range when u + 1 == CW
+#pragma unroll
+                        for (int i = 0; i < RPT; ++i) y[i][c] = fmaf(-tv[i], cf[c], y[i][c]);
+                        float s = 0.f;
+#pragma unroll
+                        for (int i = 0; i < RPT; ++i)
+                            if (i > 0 || lane > j + 1) s = fmaf(y[i][c], y[i][c], s);
+                        alpha = __shfl_sync(kFull, y[0][c], (j + 1) & 31);
+                        sig2 = warp_sum(s);
+                    }
+#pragma unroll
+                    for (int c = u + 2; c < CW; ++c)
+#pragma unroll
+                        for (int i = 0; i < RPT; ++i) y[i][c] = fmaf(-tv[i], cf[c], y[i][c]);
+                }
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) {
+                    float keep[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) keep[u] = y[i][u];
+#pragma unroll
+                    for (int c = 0; c < CW - U; ++c) y[i][c] = y[i][c + U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) y[i][CW - U + u] = keep[u];
+                }
+            }
+            shift = (U * G) % CW;
+        } else {
+            // ---- the other warps: apply H_j (later columns) or take column j
+            // of V^T V (finished columns), one barrier per step as the owner
+            const bool trailing = warp > ph;
+#pragma unroll 1
+            for (int st = 0; st < G * U; ++st) {
+                const int j = pc0 + st;
+                step_barrier(W * 32);
+                const int b = j & 1;
+                float v[RPT];
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) v[i] = S.vbuf[b][lane + 32 * i];
+                const float tau = S.taub[b];
+                float q[CW];
+#pragma unroll
+                for (int c = 0; c < CW; ++c) {
+                    q[c] = v[0] * y[0][c];
+#pragma unroll
+                    for (int i = 1; i < RPT; ++i) q[c] = fmaf(v[i], y[i][c], q[c]);
+                }
+                const float d = warp_colsum<CW>(q, scratch, lane);
+                if (trailing) {
+                    if (lane < CW) S.coef[warp][lane] = d;
+                    __syncwarp();
+                    float tv[RPT];
+#pragma unroll
+                    for (int i = 0; i < RPT; ++i) tv[i] = tau * v[i];
+#pragma unroll
+                    for (int c4 = 0; c4 < CW; c4 += 4) {
+                        const float4 w4 = *reinterpret_cast<const float4*>(&S.coef[warp][c4]);
+                        const float w[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+#pragma unroll
+                            for (int i = 0; i < RPT; ++i) y[i][c4 + e] = fmaf(-tv[i], w[e], y[i][c4 + e]);
+                    }
+                } else if (lane < CW) {
+                    const int kl = (lane + shift) % CW;
+                    if (kl < mycols) S.Sc.c[j][col0 + kl] = d;
+                }
+            }
+        }
+    }
+    step_barrier(W * 32);  // tau, rdiag and V^T V complete
+
+    // R (row r < n is lane r's slot 0 in the warp holding column k) and V
+    // below the diagonal, each warp for its own columns.
+#pragma unroll
+    for (int c = 0; c < CW; ++c) {
+        const int kl = (c + shift) % CW;
+        if (kl < mycols) {
+            const int k = col0 + kl;
+            if (lane < n) {
+                float v = (k > lane) ? y[0][c] : ((k == lane) ? S.rdiag[lane] : 0.f);
+                if (lane >= ht) v = 0.f;
+                Rt[lane + (int64_t)k * ldr] = v;
+            }
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                const int r = lane + 32 * i;
+                if (r < ht && r > k) tile[r + (int64_t)k * ld] = y[i][c];
+            }
+        }
+    }
+    // T in the top block's upper triangle (diagonal included), row i by lane
+    // i of warp 0: T(i,i) = tau_i, T(i,j) = -tau_j sum_{k=i}^{j-1} T(i,k) S(k,j).
+    if (warp == 0 && lane < n && lane < ht) {
+        const int i = lane;
+        float trow[NMAX];
+        t_factor_row<float, NMAX>(S.Sc, S.tau, i, n, trow);
+#pragma unroll
+        for (int j = 0; j < NMAX; ++j)
+            if (j >= i && j < n) tile[i + (int64_t)j * ld] = trow[j];
+    }
+    step_barrier(W * 32);  // S is reused by the CTA's next tile
+}
+
+template <int NMAX, int CW, int RPT, int MINB>
+__global__ void __launch_bounds__(32 * (NMAX / CW), MINB) factor_split_tiles(FactorParams<float> p) {
+    constexpr int B = 32 * RPT;
+    __shared__ SplitFactorSmem<NMAX, CW, RPT> S;
+    for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        const int64_t row0 = t * B;
+        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
+        factor_split_tile<NMAX, CW, RPT>(S, p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n, p.ldr);
     }
 }
 
