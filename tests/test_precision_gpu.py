@@ -33,7 +33,7 @@ def geometric_matrix(m, n, kappa, seed):
 
 
 @pytest.mark.parametrize("m,n", [(27648, 32), (4096, 16), (100000, 64), (513, 32), (1000, 7), (40, 32),
-                                 (300000, 48), (1, 1), (1024, 32)])
+                                 (300000, 48), (1, 1), (1024, 32), (262144, 16), (70001, 13)])
 def test_precision_form_matches_oracle(orc, cuda, tg, m, n):
     A = orc.fill_uniform(m, n, np.float32, seed=4)
     dA = to_dev(tg, A)

@@ -87,6 +87,20 @@ __global__ void __launch_bounds__(NT, MINB) batched_factor(const __grid_constant
     }
 }
 
+template <int NMAX, int CW, int RPT, int MINB>
+__global__ void __launch_bounds__(32 * (NMAX / CW), MINB) batched_factor_split(const __grid_constant__ FactorTable tab) {
+    constexpr int B = 32 * RPT;
+    __shared__ SplitFactorSmem<float, NMAX, CW, RPT> S;
+    for (int64_t t = blockIdx.x; t < tab.total; t += gridDim.x) {
+        const int i = find_item(tab.it, tab.count, t);
+        const FactorItem& w = tab.it[i];
+        const int64_t lt = t - w.tile0;
+        const int64_t row0 = lt * B;
+        const int ht = (int)((w.h - row0) < B ? (w.h - row0) : B);
+        factor_split_tile<float, NMAX, CW, RPT>(S, w.M + row0, w.ld, ht, w.n, w.Rout + lt * w.n, w.ldr);
+    }
+}
+
 template <int NMAX, int NT, int RPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batched_apply(const __grid_constant__ ApplyTable tab) {
     constexpr int B = NT * RPT;
@@ -102,38 +116,51 @@ __global__ void __launch_bounds__(NT, MINB) batched_apply(const __grid_constant_
     }
 }
 
-// Per-class configuration; tile heights equal those of the single-problem
-// path (tsqr.cu), so a problem's tree is the same either way.
+// Per-class configuration; tile heights and kernels equal those of the
+// single-problem path (tsqr.cu), so a problem's tree and arithmetic are the
+// same either way.
 struct ClassCfg {
-    int nmax, rows, threads;
-    size_t apply_smem;
+    int nmax, rows;
+    int factor_per_sm, apply_per_sm;  // resident CTAs per SM of each kernel
     void (*factor)(const FactorTable&, int, cudaStream_t);
     void (*apply)(const ApplyTable&, int, cudaStream_t);
 };
 
+template <int NMAX, int B, int ANT, int AMINB>
+void class_apply(const ApplyTable& t, int grid, cudaStream_t s) {
+    constexpr int ARPT = B / ANT;  // the apply CTA covers the tile height
+    constexpr size_t kSmem = apply_smem_bytes<float, NMAX, B>();
+    static bool attr = [] {
+        return cudaFuncSetAttribute(batched_apply<NMAX, ANT, ARPT, AMINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSmem) == cudaSuccess;
+    }();
+    (void)attr;
+    batched_apply<NMAX, ANT, ARPT, AMINB><<<grid, ANT, kSmem, s>>>(t);
+}
+
+// one thread per row slice (factor_tile)
 template <int NMAX, int NT, int RPT, int MINB, int AMINB, int ANT = NT>
 struct Cls {
-    static constexpr int ARPT = NT * RPT / ANT;  // the apply CTA covers the same tile height
-    static constexpr size_t kSmem = apply_smem_bytes<float, NMAX, NT * RPT>();
     static void factor(const FactorTable& t, int grid, cudaStream_t s) {
         batched_factor<NMAX, NT, RPT, MINB><<<grid, NT, 0, s>>>(t);
     }
-    static void apply(const ApplyTable& t, int grid, cudaStream_t s) {
-        static bool attr = [] {
-            return cudaFuncSetAttribute(batched_apply<NMAX, ANT, ARPT, AMINB>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem) == cudaSuccess;
-        }();
-        (void)attr;
-        batched_apply<NMAX, ANT, ARPT, AMINB><<<grid, ANT, kSmem, s>>>(t);
+    static ClassCfg cfg() { return {NMAX, NT * RPT, MINB, AMINB, &factor, &class_apply<NMAX, NT * RPT, ANT, AMINB>}; }
+};
+
+// column-split tiles (factor_split_tile)
+template <int NMAX, int CW, int RPT, int MINB, int AMINB, int ANT>
+struct SplitCls {
+    static void factor(const FactorTable& t, int grid, cudaStream_t s) {
+        batched_factor_split<NMAX, CW, RPT, MINB><<<grid, 32 * (NMAX / CW), 0, s>>>(t);
     }
-    static ClassCfg cfg() { return {NMAX, NT * RPT, NT, kSmem, &factor, &apply}; }
+    static ClassCfg cfg() { return {NMAX, 32 * RPT, MINB, AMINB, &factor, &class_apply<NMAX, 32 * RPT, ANT, AMINB>}; }
 };
 
 const ClassCfg& class_of(int n) {
     static const ClassCfg c8 = Cls<8, 256, 4, 3, 3>::cfg();
-    static const ClassCfg c16 = Cls<16, 256, 2, 2, 3>::cfg();
-    static const ClassCfg c32 = Cls<32, 128, 4, 2, 2, 256>::cfg();
-    static const ClassCfg c64 = Cls<64, 128, 2, 2, 1, 256>::cfg();
+    static const ClassCfg c16 = SplitCls<16, 4, 16, 4, 3, 256>::cfg();
+    static const ClassCfg c32 = SplitCls<32, 4, 16, 2, 2, 256>::cfg();
+    static const ClassCfg c64 = SplitCls<64, 8, 16, 1, 1, 256>::cfg();
     if (n <= 8) return c8;
     if (n <= 16) return c16;
     if (n <= 32) return c32;
@@ -170,7 +197,7 @@ int resident_grid(const ClassCfg& c, bool apply, int64_t tiles) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 148;
     }
-    const int per_sm = (apply && c.nmax >= 64) ? 1 : 2;  // resident CTAs per SM of each configuration
+    const int per_sm = apply ? c.apply_per_sm : c.factor_per_sm;
     return (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * per_sm));
 }
 

@@ -251,6 +251,8 @@ bool tc_apply_level(const ApplyParams<float>& p, int nmax, int rows, int* err, c
     const int grid = (int)(p.ntiles < 1 ? 1 : (p.ntiles > resident ? resident : p.ntiles));
     if (nmax == 32 && rows == 512) {
         launch<32, 512>(p, grid, err, s);
+    } else if (nmax == 16 && rows == 512) {
+        launch<16, 512>(p, grid, err, s);
     } else {
         return false;
     }

@@ -42,18 +42,18 @@ struct TileCfg {
     }
 };
 
-// FP32 factor on column-split tiles (factor_split_tiles: NMAX/CW warps per
+// Factor on column-split tiles (factor_split_tiles: NMAX/CW warps per
 // 32*RPT-row tile), with the same apply kernel as TileCfg.
-template <int NMAX, int CW, int RPT, int MINB, int ANT, int AMINB>
+template <typename T, int NMAX, int CW, int RPT, int MINB, int ANT, int AMINB>
 struct SplitCfg {
     static constexpr int kRows = 32 * RPT;
     static constexpr int ARPT = kRows / ANT;
     static_assert(kRows % ANT == 0, "apply block must divide the tile");
-    static void factor(const FactorParams<float>& p, int grid, cudaStream_t s) {
-        factor_split_tiles<NMAX, CW, RPT, MINB><<<grid, 32 * (NMAX / CW), 0, s>>>(p);
+    static void factor(const FactorParams<T>& p, int grid, cudaStream_t s) {
+        factor_split_tiles<T, NMAX, CW, RPT, MINB><<<grid, 32 * (NMAX / CW), 0, s>>>(p);
     }
-    static void apply(const ApplyParams<float>& p, int grid, cudaStream_t s) {
-        TileCfg<float, NMAX, ANT, ARPT, 1, AMINB>::apply(p, grid, s);
+    static void apply(const ApplyParams<T>& p, int grid, cudaStream_t s) {
+        TileCfg<T, NMAX, ANT, ARPT, 1, AMINB>::apply(p, grid, s);
     }
 };
 
@@ -77,18 +77,22 @@ KernelSet<T> make_set() {
 // times n; B >= 4n keeps the stacked-R levels at most a quarter of the level
 // below, and the tile stays in registers (RPT rows x NMAX columns/thread).
 KernelSet<float> pick(float*, int n) {
+    // Level-0 factor times at 4,194,304 rows, column-split (factor_split_tiles)
+    // against the earlier one-thread-per-row-slice kernel (factor_tiles):
+    // n = 16: 0.20 vs 0.49 ms; n = 32: 0.72 vs 0.98 ms; n = 64: 3.2 vs 5.7 ms.
+    // n = 64 keeps 512-row tiles (whole TSQR 6.9 ms, vs 9.9 ms with 256-row
+    // tiles, whose stacked-R level is twice as tall).
     if (n <= 8) return make_set<TileCfg<float, 8, 256, 4, 3, 3>, float>();
-    if (n <= 16) return make_set<TileCfg<float, 16, 256, 2, 2, 3>, float>();
-    // n <= 32: 8 warps of 4 columns x 512 rows (0.74 ms for the level-0
-    // factor at 4,194,304 x 32, vs 0.98 ms for 4 warps of 128 full rows)
-    if (n <= 32) return make_set<SplitCfg<32, 4, 16, 2, 256, 2>, float>();
-    if (n <= 64) return make_set<TileCfg<float, 64, 128, 2, 2, 1, 256>, float>();
+    if (n <= 16) return make_set<SplitCfg<float, 16, 4, 16, 4, 256, 3>, float>();
+    if (n <= 32) return make_set<SplitCfg<float, 32, 4, 16, 2, 256, 2>, float>();
+    if (n <= 64) return make_set<SplitCfg<float, 64, 8, 16, 1, 256, 1>, float>();
     return KernelSet<float>();
 }
 KernelSet<double> pick(double*, int n) {
+    // n = 32 at 2,097,152 rows: 7.5 ms (column-split) vs 19.0 ms
     if (n <= 8) return make_set<TileCfg<double, 8, 256, 2, 2, 3>, double>();
     if (n <= 16) return make_set<TileCfg<double, 16, 256, 2, 1, 2>, double>();
-    if (n <= 32) return make_set<TileCfg<double, 32, 256, 1, 1, 2>, double>();
+    if (n <= 32) return make_set<SplitCfg<double, 32, 4, 8, 3, 256, 2>, double>();
     return KernelSet<double>();
 }
 
@@ -215,12 +219,15 @@ PrecCfg pick_precision(int n) {
     // at 2.7x the FP32 factor time on GB300's FP64 pipe (4.66 ms vs 1.73 ms
     // at 4,194,304 x 32) with no gain in the error figures, so the FP64 part
     // of this form is the root combine only.
-    if (n <= 32) {
+    if (n <= 16) {
+        c.nmax = 16;
+        c.ks = make_set<SplitCfg<float, 16, 4, 16, 4, 256, 3>, float>();
+    } else if (n <= 32) {
         c.nmax = 32;
-        c.ks = make_set<SplitCfg<32, 4, 16, 2, 256, 2>, float>();
+        c.ks = make_set<SplitCfg<float, 32, 4, 16, 2, 256, 2>, float>();
     } else if (n <= 64) {
         c.nmax = 64;
-        c.ks = make_set<TileCfg<float, 64, 128, 2, 2, 1, 256>, float>();
+        c.ks = make_set<SplitCfg<float, 64, 8, 16, 1, 256, 1>, float>();
     }
     c.rows = c.ks.rows;
     return c;

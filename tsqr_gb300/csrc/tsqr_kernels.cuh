@@ -542,41 +542,71 @@ __global__ void __launch_bounds__(32 * WPB, MINB) factor_warp_tiles(FactorParams
 }
 
 // ---------------------------------------------------------------------------
-// Column-split tiles (FP32, n <= NMAX <= 32, tiles of 32*RPT rows).  The W = NMAX/CW
-// warps of a CTA share one tile: warp w holds columns [w*CW, w*CW + CW) of
-// all 32*RPT rows (row lane + 32*i in y[i]), so a thread carries RPT*CW
-// tile values instead of RPT*NMAX.  Column j
-// is owned by warp j/CW.  At step j the owner forms v_j and tau_j from its
-// column, publishes them to shared memory and passes one CTA barrier; then
-// every warp applies H_j to its own columns (dot products, a per-warp
-// transpose reduction, the rank-1 update) while the owner goes on to column
-// j+1.  Warps whose columns are all finished only take the dot products that
-// give column j of V^T V.  The critical path of a step is the owner's chain
-// for one CW-column block instead of the whole tile.  v_j alternates between
-// two buffers: the owner rewrites buffer b at step j+2, after every warp has
-// passed the barrier of step j+1 and so has read step j's copy.
+// Column-split tiles (n <= NMAX <= 64, tiles of 32*RPT rows, FP32 or FP64).
+// The W = NMAX/CW warps of a CTA share one tile: warp w holds columns
+// [w*CW, w*CW + CW) of all 32*RPT rows (row lane + 32*i in y[i]), so a
+// thread carries RPT*CW tile values instead of RPT*NMAX and more rows fit on
+// an SM.  Column j is owned by warp j/CW.  At step j the owner forms v_j and
+// tau_j from its column, publishes them to shared memory and passes one CTA
+// barrier; then every warp applies H_j to its own columns (dot products, a
+// per-warp transpose reduction, the rank-1 update) while the owner goes on to
+// column j+1.  Warps whose columns are all finished only take the dot
+// products that give column j of V^T V.  The critical path of a step is the
+// owner's chain for one CW-column block instead of the whole tile.  v_j
+// alternates between two buffers: the owner rewrites buffer b at step j+2,
+// after every warp has passed the barrier of step j+1 and so has read step
+// j's copy.
 //
 // Every warp executes the same number of barriers (one per step; a phase of
 // nloc columns runs 4*ceil(nloc/4) steps, the padding steps act on zero
 // columns with tau = 0).  Output format as factor_tile.
-// Row stride of the per-warp transpose scratch: CW = 4 needs no padding
-// (lane l's 16-byte row is words 4l..4l+3, and the column reads of the 8
-// lanes per position hit 32 distinct banks); wider rows get 4 words of pad.
-template <int CW>
+
+__device__ __forceinline__ float fmadd(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmadd(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float sqrt_t(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrt_t(double x) { return sqrt(x); }
+
+// 16-byte vector of T.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    static constexpr int N = 4;
+    __device__ static void store(float* p, const float* v) { *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]); }
+    __device__ static void load(const float* p, float* v) {
+        const float4 q = *reinterpret_cast<const float4*>(p);
+        v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+    }
+};
+template <>
+struct Vec16<double> {
+    static constexpr int N = 2;
+    __device__ static void store(double* p, const double* v) { *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]); }
+    __device__ static void load(const double* p, double* v) {
+        const double2 q = *reinterpret_cast<const double2*>(p);
+        v[0] = q.x, v[1] = q.y;
+    }
+};
+
+// Row stride (elements) of the per-warp transpose scratch.  FP32 with CW = 4
+// needs no padding (lane l's 16-byte row is words 4l..4l+3, and the column
+// reads of the 8 lanes per position hit 32 distinct banks); other shapes
+// get 16 bytes of pad.
+template <typename T, int CW>
 __host__ __device__ constexpr int colsum_stride() {
-    return CW == 4 ? 4 : CW + 4;
+    return (sizeof(T) == 4 && CW == 4) ? 4 : CW + 16 / (int)sizeof(T);
 }
 
-template <int NMAX, int CW, int RPT>
+template <typename T, int NMAX, int CW, int RPT>
 struct SplitFactorSmem {
     static constexpr int W = NMAX / CW;
-    __align__(16) float vbuf[2][32 * RPT];
-    float taub[2];
-    __align__(16) float xpose[W][32 * colsum_stride<CW>()];
-    __align__(16) float coef[W][CW];
-    SCols<float, NMAX> Sc;
-    float tau[NMAX];
-    float rdiag[NMAX];
+    __align__(16) T vbuf[2][32 * RPT];
+    T taub[2];
+    __align__(16) T xpose[W][32 * colsum_stride<T, CW>()];
+    __align__(16) T coef[W][CW];
+    SCols<T, NMAX> Sc;
+    T tau[NMAX];
+    T rdiag[NMAX];
 };
 
 // CTA barrier 1 over `count` threads; non-aligned form, since the owner and
@@ -588,49 +618,60 @@ __device__ __forceinline__ void step_barrier(int count) {
 // Sum CW per-lane partials over the warp through a shared-memory transpose:
 // returns, in lane l, the full sum of position l % CW (32/CW lanes hold each
 // sum, bitwise equal).
-template <int CW>
-__device__ __forceinline__ float warp_colsum(const float (&q)[CW], float* scratch, int lane) {
-    constexpr int SP = colsum_stride<CW>();
+template <typename T, int CW>
+__device__ __forceinline__ T warp_colsum(const T (&q)[CW], T* scratch, int lane) {
+    constexpr int SP = colsum_stride<T, CW>();
+    constexpr int VN = Vec16<T>::N;
     constexpr int LPP = 32 / CW;  // lanes per position
     constexpr int RPL = 32 / LPP;  // rows summed by one lane
-    float* mine = scratch + lane * SP;
+    T* mine = scratch + lane * SP;
 #pragma unroll
-    for (int c = 0; c < CW; c += 4) *reinterpret_cast<float4*>(mine + c) = make_float4(q[c], q[c + 1], q[c + 2], q[c + 3]);
+    for (int c = 0; c < CW; c += VN) Vec16<T>::store(mine + c, &q[c]);
     __syncwarp();
     const int p = lane % CW, h = lane / CW;
-    float a[RPL];
+    T a[RPL];
 #pragma unroll
     for (int r = 0; r < RPL; ++r) a[r] = scratch[(h + LPP * r) * SP + p];
 #pragma unroll
     for (int w = RPL / 2; w >= 1; w >>= 1)
 #pragma unroll
         for (int r = 0; r < w; ++r) a[r] += a[r + w];
-    float s = a[0];
+    T s = a[0];
 #pragma unroll
     for (int o = CW; o < 32; o <<= 1) s += __shfl_xor_sync(kFull, s, o);
     __syncwarp();  // scratch is rewritten by the next call
     return s;
 }
 
-template <int NMAX, int CW, int RPT>
-__device__ __forceinline__ void factor_split_tile(SplitFactorSmem<NMAX, CW, RPT>& S, float* tile, int64_t ld, int ht,
-                                                  int n, float* Rt, int64_t ldr) {
+template <typename T, int NMAX, int CW, int RPT>
+__device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, RPT>& S, T* tile, int64_t ld, int ht,
+                                                  int n, T* Rt, int64_t ldr) {
     constexpr int W = NMAX / CW;
     constexpr int U = 4;
-    static_assert(NMAX <= 32 && CW % U == 0 && NMAX % CW == 0 && W >= 2, "bad split configuration");
+    constexpr int VN = Vec16<T>::N;
+    static_assert(NMAX <= 64 && CW % U == 0 && CW % VN == 0 && NMAX % CW == 0 && W >= 2 && 32 * RPT >= NMAX &&
+                      W >= NMAX / 32,
+                  "bad split configuration");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int col0 = warp * CW;
     const int mycols = max(0, min(CW, n - col0));
-    float* scratch = S.xpose[warp];
+    T* scratch = S.xpose[warp];
+    // Row lane + 32*i lies strictly below diagonal element j (compile-time
+    // true for every slot i >= 1 when NMAX <= 32).
+    auto below = [&](int i, int j) { return (NMAX <= 32 && i > 0) || (lane + 32 * i > j); };
+    // x(j, c) of position c, held by lane j % 32 in slot j / 32 (j < 64)
+    auto diag_slot = [&](const T(&yy)[RPT][CW], int c, int j) {
+        return (NMAX > 32 && j >= 32) ? yy[RPT > 1 ? 1 : 0][c] : yy[0][c];
+    };
 
-    float y[RPT][CW];
+    T y[RPT][CW];
     {
         // one column pointer stepped by ld; the row offsets 32*i are immediates
-        const float* pcol = tile + (int64_t)col0 * ld + lane;
+        const T* pcol = tile + (int64_t)col0 * ld + lane;
 #pragma unroll
         for (int c = 0; c < CW; ++c) {
 #pragma unroll
-            for (int i = 0; i < RPT; ++i) y[i][c] = (lane + 32 * i < ht && c < mycols) ? pcol[32 * i] : 0.f;
+            for (int i = 0; i < RPT; ++i) y[i][c] = (lane + 32 * i < ht && c < mycols) ? pcol[32 * i] : T(0);
             pcol += ld;
         }
     }
@@ -646,13 +687,13 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<NMAX, CW, RPT>
             // ---- owner: reflectors of columns pc0 .. pc0+nloc-1, in groups of
             // U with the register rotation of factor_tile, and the norm of the
             // next column reduced while the current update is issued
-            float sig2, alpha;
+            T sig2, alpha;
             {
-                float s = 0.f;
+                T s = 0;
 #pragma unroll
                 for (int i = 0; i < RPT; ++i)
-                    if (i > 0 || lane > pc0) s = fmaf(y[i][0], y[i][0], s);
-                alpha = __shfl_sync(kFull, y[0][0], pc0 & 31);
+                    if (below(i, pc0)) s = fmadd(y[i][0], y[i][0], s);
+                alpha = __shfl_sync(kFull, diag_slot(y, 0, pc0), pc0 & 31);
                 sig2 = warp_sum(s);
             }
 #pragma unroll 1
@@ -663,73 +704,68 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<NMAX, CW, RPT>
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int j = pc0 + base + u;
-                    const bool zero = (sig2 == 0.f);
-                    const float nrm = sqrtf(fmaf(alpha, alpha, sig2));
-                    const float beta = zero ? alpha : ((alpha >= 0.f) ? -nrm : nrm);
-                    const float tau = zero ? 0.f : (beta - alpha) * recip(beta);
-                    const float scale = zero ? 0.f : recip(alpha - beta);
+                    const bool zero = (sig2 == T(0));
+                    const T nrm = sqrt_t(fmadd(alpha, alpha, sig2));
+                    const T beta = zero ? alpha : ((alpha >= T(0)) ? -nrm : nrm);
+                    const T tau = zero ? T(0) : (beta - alpha) * recip(beta);
+                    const T scale = zero ? T(0) : recip(alpha - beta);
 #pragma unroll
                     for (int i = 0; i < RPT; ++i)
-                        if (i > 0 || lane > j) y[i][u] *= scale;
-                    const float v0 = (lane > j) ? y[0][u] : ((lane == j) ? 1.f : 0.f);
+                        if (below(i, j)) y[i][u] *= scale;
+                    // v_j of slot i (1 on the diagonal, 0 above it)
+                    auto vj = [&](int i) { return below(i, j) ? y[i][u] : ((lane + 32 * i == j) ? T(1) : T(0)); };
                     const int b = j & 1;
-                    S.vbuf[b][lane] = v0;
 #pragma unroll
-                    for (int i = 1; i < RPT; ++i) S.vbuf[b][lane + 32 * i] = y[i][u];
+                    for (int i = 0; i < RPT; ++i) S.vbuf[b][lane + 32 * i] = vj(i);
                     if (lane == 0) {
                         S.taub[b] = tau;
                         S.tau[j] = tau;
                         S.rdiag[j] = beta;
                     }
                     step_barrier(W * 32);
-                    float q[CW];
+                    T q[CW];
 #pragma unroll
                     for (int c = 0; c < CW; ++c) {
-                        q[c] = (c != u) ? v0 * y[0][c] : 0.f;
+                        q[c] = (c != u) ? vj(0) * y[0][c] : T(0);
 #pragma unroll
                         for (int i = 1; i < RPT; ++i)
-                            if (c != u) q[c] = fmaf(y[i][u], y[i][c], q[c]);
+                            if (c != u) q[c] = fmadd(vj(i), y[i][c], q[c]);
                     }
-                    const float d = warp_colsum<CW>(q, scratch, lane);
+                    const T d = warp_colsum<T, CW>(q, scratch, lane);
                     if (lane < CW) {
-                        S.coef[warp][lane] = (lane > u && lane < live) ? d : 0.f;
+                        S.coef[warp][lane] = (lane > u && lane < live) ? d : T(0);
                         const int k = (lane >= past0) ? lane - past0 : ((lane < u) ? base + lane : -1);
                         if (k >= 0) S.Sc.c[j][pc0 + k] = d;
                     }
                     __syncwarp();
-                    float tv[RPT];
-                    tv[0] = tau * v0;
+                    T tv[RPT];
 #pragma unroll
-                    for (int i = 1; i < RPT; ++i) tv[i] = tau * y[i][u];
-                    float cf[CW];
+                    for (int i = 0; i < RPT; ++i) tv[i] = tau * vj(i);
+                    T cf[CW];
 #pragma unroll
-                    for (int c4 = 0; c4 < CW; c4 += 4) {
-                        if (c4 + 3 <= u) continue;
-                        const float4 w4 = *reinterpret_cast<const float4*>(&S.coef[warp][c4]);
-                        cf[c4] = w4.x;
-                        cf[c4 + 1] = w4.y;
-                        cf[c4 + 2] = w4.z;
-                        cf[c4 + 3] = w4.w;
+                    for (int c0 = 0; c0 < CW; c0 += VN) {
+                        if (c0 + VN - 1 <= u) continue;
+                        Vec16<T>::load(&S.coef[warp][c0], &cf[c0]);
                     }
                     if (u + 1 < CW) {
                         const int c = (u + 1 < CW) ? u + 1 : 0;  // keeps the index in range when u + 1 == CW
 #pragma unroll
-                        for (int i = 0; i < RPT; ++i) y[i][c] = fmaf(-tv[i], cf[c], y[i][c]);
-                        float s = 0.f;
+                        for (int i = 0; i < RPT; ++i) y[i][c] = fmadd(-tv[i], cf[c], y[i][c]);
+                        T s = 0;
 #pragma unroll
                         for (int i = 0; i < RPT; ++i)
-                            if (i > 0 || lane > j + 1) s = fmaf(y[i][c], y[i][c], s);
-                        alpha = __shfl_sync(kFull, y[0][c], (j + 1) & 31);
+                            if (below(i, j + 1)) s = fmadd(y[i][c], y[i][c], s);
+                        alpha = __shfl_sync(kFull, diag_slot(y, c, j + 1), (j + 1) & 31);
                         sig2 = warp_sum(s);
                     }
 #pragma unroll
                     for (int c = u + 2; c < CW; ++c)
 #pragma unroll
-                        for (int i = 0; i < RPT; ++i) y[i][c] = fmaf(-tv[i], cf[c], y[i][c]);
+                        for (int i = 0; i < RPT; ++i) y[i][c] = fmadd(-tv[i], cf[c], y[i][c]);
                 }
 #pragma unroll
                 for (int i = 0; i < RPT; ++i) {
-                    float keep[U];
+                    T keep[U];
 #pragma unroll
                     for (int u = 0; u < U; ++u) keep[u] = y[i][u];
 #pragma unroll
@@ -748,32 +784,32 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<NMAX, CW, RPT>
                 const int j = pc0 + st;
                 step_barrier(W * 32);
                 const int b = j & 1;
-                float v[RPT];
+                T v[RPT];
 #pragma unroll
                 for (int i = 0; i < RPT; ++i) v[i] = S.vbuf[b][lane + 32 * i];
-                const float tau = S.taub[b];
-                float q[CW];
+                const T tau = S.taub[b];
+                T q[CW];
 #pragma unroll
                 for (int c = 0; c < CW; ++c) {
                     q[c] = v[0] * y[0][c];
 #pragma unroll
-                    for (int i = 1; i < RPT; ++i) q[c] = fmaf(v[i], y[i][c], q[c]);
+                    for (int i = 1; i < RPT; ++i) q[c] = fmadd(v[i], y[i][c], q[c]);
                 }
-                const float d = warp_colsum<CW>(q, scratch, lane);
+                const T d = warp_colsum<T, CW>(q, scratch, lane);
                 if (trailing) {
                     if (lane < CW) S.coef[warp][lane] = d;
                     __syncwarp();
-                    float tv[RPT];
+                    T tv[RPT];
 #pragma unroll
                     for (int i = 0; i < RPT; ++i) tv[i] = tau * v[i];
 #pragma unroll
-                    for (int c4 = 0; c4 < CW; c4 += 4) {
-                        const float4 w4 = *reinterpret_cast<const float4*>(&S.coef[warp][c4]);
-                        const float w[4] = {w4.x, w4.y, w4.z, w4.w};
+                    for (int c0 = 0; c0 < CW; c0 += VN) {
+                        T w[VN];
+                        Vec16<T>::load(&S.coef[warp][c0], w);
 #pragma unroll
-                        for (int e = 0; e < 4; ++e)
+                        for (int e = 0; e < VN; ++e)
 #pragma unroll
-                            for (int i = 0; i < RPT; ++i) y[i][c4 + e] = fmaf(-tv[i], w[e], y[i][c4 + e]);
+                            for (int i = 0; i < RPT; ++i) y[i][c0 + e] = fmadd(-tv[i], w[e], y[i][c0 + e]);
                     }
                 } else if (lane < CW) {
                     const int kl = (lane + shift) % CW;
@@ -784,17 +820,21 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<NMAX, CW, RPT>
     }
     step_barrier(W * 32);  // tau, rdiag and V^T V complete
 
-    // R (row r < n is lane r's slot 0 in the warp holding column k) and V
-    // below the diagonal, each warp for its own columns.
+    // R (row r < n sits in slot r / 32 of lane r % 32 in the warp holding
+    // column k) and V below the diagonal, each warp for its own columns.
 #pragma unroll
     for (int c = 0; c < CW; ++c) {
         const int kl = (c + shift) % CW;
         if (kl < mycols) {
             const int k = col0 + kl;
-            if (lane < n) {
-                float v = (k > lane) ? y[0][c] : ((k == lane) ? S.rdiag[lane] : 0.f);
-                if (lane >= ht) v = 0.f;
-                Rt[lane + (int64_t)k * ldr] = v;
+#pragma unroll
+            for (int i = 0; i < (NMAX + 31) / 32; ++i) {
+                const int r = lane + 32 * i;
+                if (r < n) {
+                    T v = (k > r) ? y[i][c] : ((k == r) ? S.rdiag[r] : T(0));
+                    if (r >= ht) v = T(0);
+                    Rt[r + (int64_t)k * ldr] = v;
+                }
             }
 #pragma unroll
             for (int i = 0; i < RPT; ++i) {
@@ -803,27 +843,29 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<NMAX, CW, RPT>
             }
         }
     }
-    // T in the top block's upper triangle (diagonal included), row i by lane
-    // i of warp 0: T(i,i) = tau_i, T(i,j) = -tau_j sum_{k=i}^{j-1} T(i,k) S(k,j).
-    if (warp == 0 && lane < n && lane < ht) {
-        const int i = lane;
-        float trow[NMAX];
-        t_factor_row<float, NMAX>(S.Sc, S.tau, i, n, trow);
+    // T in the top block's upper triangle (diagonal included), row i by
+    // thread i: T(i,i) = tau_i, T(i,j) = -tau_j sum_{k=i}^{j-1} T(i,k) S(k,j).
+    {
+        const int i = threadIdx.x;
+        if (i < n && i < ht) {
+            T trow[NMAX];
+            t_factor_row<T, NMAX>(S.Sc, S.tau, i, n, trow);
 #pragma unroll
-        for (int j = 0; j < NMAX; ++j)
-            if (j >= i && j < n) tile[i + (int64_t)j * ld] = trow[j];
+            for (int j = 0; j < NMAX; ++j)
+                if (j >= i && j < n) tile[i + (int64_t)j * ld] = trow[j];
+        }
     }
     step_barrier(W * 32);  // S is reused by the CTA's next tile
 }
 
-template <int NMAX, int CW, int RPT, int MINB>
-__global__ void __launch_bounds__(32 * (NMAX / CW), MINB) factor_split_tiles(FactorParams<float> p) {
+template <typename T, int NMAX, int CW, int RPT, int MINB>
+__global__ void __launch_bounds__(32 * (NMAX / CW), MINB) factor_split_tiles(FactorParams<T> p) {
     constexpr int B = 32 * RPT;
-    __shared__ SplitFactorSmem<NMAX, CW, RPT> S;
+    __shared__ SplitFactorSmem<T, NMAX, CW, RPT> S;
     for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
         const int64_t row0 = t * B;
         const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
-        factor_split_tile<NMAX, CW, RPT>(S, p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n, p.ldr);
+        factor_split_tile<T, NMAX, CW, RPT>(S, p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n, p.ldr);
     }
 }
 
