@@ -2,6 +2,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--m M] [--n N] [--form auto|plain|tf32x3|bf16x3]
+                    [--workload tsqr|batch|qr] [--dtype f32|f64] [--reorth]
 
 One step = one TSQR (A <- Q, R) of the whole matrix through libtsqr_gb300's C
 ABI.  Input: A = U diag(sigma) V^T with U, V orthonormal (QR of seeded
@@ -22,6 +23,11 @@ Printed (rank 0, one JSON line):
                on the host cores, on the same workload
   forms        each precision form's time and FP64-checked errors
 
+--workload batch: 512 uneven FP32 problems through the batched entry point,
+replayed from one CUDA graph, against a loop of single calls (problems/s).
+--workload qr: the recursive blocked QR (qr<T>) at --m x --n in --dtype, every
+form timed, FP64-checked errors per form.
+
 --impl reference: the reference has no CPU path and its own code is CUDA, so
 this arm times the oracle's restatement of the reference algorithm
 (TallShinnyQR.h:86-148 schedule, kernelQR.h:69-291 tile QR, FP32) on all host
@@ -29,6 +35,7 @@ cores of rank 0, on the same workload; other ranks exit without work.
 """
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -39,6 +46,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "QR TFLOP/s & % roofline, tensor-core vs plain FP32 at equal FP64-oracle error"
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# level-0 kernels at 4,194,304 x 32: one ncu --set full capture of each kernel
+# at 2,097,152 rows (factor 495.0 MB, tensor-core apply 492.6 MB, CUDA-core
+# apply 491.9 MB), scaled by the tile count (x2).
+TRAFFIC = {(4194304, 32, "factor_level0"): 2 * 495.0e6,
+           (4194304, 32, "tc_level0"): 2 * 492.6e6,
+           (4194304, 32, "apply_level0"): 2 * 491.9e6}
+TRAFFIC_SOURCE = "ncu capture at 2,097,152 rows, x2 for the tile count"
 
 
 def flops(m, n):
@@ -325,6 +341,47 @@ def run_batch(tg, steps, warmup, device, seed=2024):
     return out
 
 
+def run_qr(tg, m, n, dtype, forms, reorth, steps, warmup, device, kappa=1e4, seed=77):
+    """Recursive blocked QR (qr_, the reference's qr<T>) of A = U diag(sigma)
+    V^T with sigma geometric 1 -> 1/kappa: every form timed with CUDA events
+    on its stream (A restored and L2 flushed before each step, outside the
+    timed pair), then FP64 backward error and orthogonality."""
+    import torch
+    g = torch.Generator(device=device).manual_seed(seed)
+    U = orthonormal_columns(torch.randn((m, n), generator=g, device=device, dtype=torch.float64))
+    V = orthonormal_columns(torch.randn((n, n), generator=g, device=device, dtype=torch.float64))
+    sig = torch.logspace(0, -math.log10(kappa), n, device=device, dtype=torch.float64)
+    A0 = ((U * sig) @ V.t()).to(dtype).t().contiguous().t()
+    del U
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    out = {}
+    for f in forms:
+        A = A0.t().clone().t()
+        R = tg.empty_colmajor(n, n, dtype, device)
+        nb = tg.qr_workspace_bytes(m, n, dtype, precision=f, reorth=reorth)
+        if nb == 0:
+            out[f] = {"unavailable": "form not offered for this dtype/shape"}
+            continue
+        work = torch.empty(nb, dtype=torch.uint8, device=device)
+        stream = torch.cuda.Stream(device=device)
+        ts = []
+        for k in range(warmup + steps):
+            with torch.cuda.stream(stream):
+                A.copy_(A0)
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                tg.qr_(A, R, precision=f, reorth=reorth, work=work, stream=stream)
+                b.record(stream)
+            stream.synchronize()
+            if k >= warmup:
+                ts.append(a.elapsed_time(b))
+        back, orth = check_errors(A0, A, R)
+        msx = sum(ts) / len(ts)
+        out[f] = {"ms": msx, "tflops": flops(m, n) / (msx * 1e-3) / 1e12, "backward": back, "orth": orth}
+    return out
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -342,7 +399,10 @@ def main():
     ap.add_argument("--n", type=int, default=32)
     ap.add_argument("--form", default="auto")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="tsqr", choices=["tsqr", "batch"])
+    ap.add_argument("--workload", default="tsqr", choices=["tsqr", "batch", "qr"])
+    ap.add_argument("--dtype", default="f32", choices=["f32", "f64"], help="qr workload only")
+    ap.add_argument("--reorth", action="store_true", help="qr workload: one reorthogonalisation pass")
+    ap.add_argument("--kappa", type=float, default=1e4, help="qr workload: condition number of A")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
@@ -407,6 +467,28 @@ def main():
             print(json.dumps(out))
         return 0
 
+    if args.workload == "qr":
+        dt = torch.float32 if args.dtype == "f32" else torch.float64
+        forms = (["plain", "tf32x3"] if args.dtype == "f32" else ["plain"]) if args.form == "auto" else [args.form]
+        sampler = ClockSampler(local)
+        sampler.start()
+        res = run_qr(tg, m, n, dt, forms, args.reorth, args.steps, args.warmup, device, kappa=args.kappa)
+        clocks = sampler.stop()
+        bar = 1e-5 if args.dtype == "f32" else 1e-12
+        ok = {f: r for f, r in res.items() if "ms" in r and r["backward"] <= bar}
+        head = min(ok, key=lambda f: ok[f]["ms"]) if ok else forms[0]
+        r = res[head]
+        out = {"metric": "blocked QR TFLOP/s (geqrf+orgqr flops)", "value": r.get("tflops"), "unit": "TFLOP/s",
+               "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r.get("ms"),
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+               "data": "synthetic: A = U diag(sigma) V^T, sigma geometric 1..1/%g, seeded" % args.kappa,
+               "config": {"workload": "recursive blocked QR (qr<T>) m=%d n=%d reorth=%s" % (m, n, args.reorth),
+                          "form": head, "l2": "flushed (256 MiB write) before every step"},
+               "forms": res, "clocks": clocks}
+        if rank == 0:
+            print(json.dumps(out))
+        return 0
+
     A0 = make_input(m, n, 1234 + rank, device)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
     forms = ["plain", "tf32x3"] if args.form == "auto" else [args.form]
@@ -440,9 +522,13 @@ def main():
     kind = dom_tag // 1000
     level = dom_tag % 1000
     # algorithmic bytes of a level-0 launch: the tile data read + written once
-    # (factor: A in, V out; apply: V in, Q out) plus the n x n per tile R/B.
-    dom_bytes = 2.0 * m * n * 4 if level == 0 else None
+    # (factor: A in, V out; apply: V in, Q out) plus the n x n R (factor) or
+    # parent block (apply) of every tile of B rows.
+    tile_rows = 1024 if n <= 8 else 512
+    dom_bytes = (2.0 * m * n + -(-m // tile_rows) * n * n) * 4 if level == 0 else None
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9 if dom_bytes else None
+    dom_name = ("factor" if kind == 1 else "apply" if kind == 2 else "tc") + "_level%d" % level
+    traffic = TRAFFIC.get((m, n, dom_name))
     roof_t = max(F / (fp32_peak * 1e12), alg_bytes(m, n) / (pk["hbm_gbs"] * 1e9))
     e2e = run_e2e(tg, A0, head, max(3, args.steps // 4), 2, device)
     e2e_val = ws * F / (e2e["ms"] * 1e-3) / 1e12
@@ -463,9 +549,10 @@ def main():
                    "input_restore": "A restored from a pristine copy before every step, outside the timed pair"},
         "errors": {"backward": r["backward"], "orth": r["orth"], "bar": 1e-5},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": None,
-                     "kernel": ("factor" if kind == 1 else "apply" if kind == 2 else "tc") + "_level%d" % level,
-                     "kernel_ms": dom_ms, "peak_source": pk["source"]},
+                     "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
+                     "traffic": traffic, "traffic_source": TRAFFIC_SOURCE if traffic else None,
+                     "algorithmic_bytes": dom_bytes, "kernel": dom_name, "kernel_ms": dom_ms,
+                     "peak_source": pk["source"]},
         "step_roofline": {"time_ms": roof_t * 1e3, "frac": roof_t * 1e3 / ms, "fp32_peak_tflops": fp32_peak,
                           "fp32_peak_source": "nominal: SMs x 128 lanes x 2 x max SM clock",
                           "hbm_gbs": pk["hbm_gbs"], "flops": F, "bytes": alg_bytes(m, n)},
