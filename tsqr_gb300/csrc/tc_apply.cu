@@ -92,18 +92,29 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
         float* tile = p.M + row0;
 
         // --- W = T (V_top^T B) on CUDA cores, then W as the B operand -----
-        for (int idx = tid; idx < NMAX * NMAX; idx += 128) {
-            const int r = idx % NMAX, c = idx / NMAX;
-            const bool in = (r < ht && r < n && c < n);
-            const float v = in ? tile[r + c * p.ld] : 0.f;
-            S.Vt[r][c] = (r > c) ? v : ((r == c && c < n) ? 1.f : 0.f);
-            S.u.w.Tt[r][c] = (r <= c) ? v : 0.f;
-            float b;
-            if (p.P)
-                b = (r < n && c < n) ? p.P[t * n + r + c * p.ldp] : 0.f;
-            else
-                b = (r == c && r < n) ? 1.f : 0.f;
-            S.Bs[r][c] = b;
+        {
+            // all global reads first: interleaved with the shared stores they
+            // would be issued one at a time (the generic pointers may alias)
+            constexpr int PER = NMAX * NMAX / 128;
+            float tv[PER], bv[PER];
+#pragma unroll
+            for (int e = 0; e < PER; ++e) {
+                const int idx = tid + 128 * e;
+                const int r = idx % NMAX, c = idx / NMAX;
+                tv[e] = (r < ht && r < n && c < n) ? tile[r + c * p.ld] : 0.f;
+                if (p.P)
+                    bv[e] = (r < n && c < n) ? p.P[t * n + r + c * p.ldp] : 0.f;
+                else
+                    bv[e] = (r == c && r < n) ? 1.f : 0.f;
+            }
+#pragma unroll
+            for (int e = 0; e < PER; ++e) {
+                const int idx = tid + 128 * e;
+                const int r = idx % NMAX, c = idx / NMAX;
+                S.Vt[r][c] = (r > c) ? tv[e] : ((r == c && c < n) ? 1.f : 0.f);
+                S.u.w.Tt[r][c] = (r <= c) ? tv[e] : 0.f;
+                S.Bs[r][c] = bv[e];
+            }
         }
         __syncthreads();
         // Each thread owns output row k and CPT columns c0 + CS*j: CPT

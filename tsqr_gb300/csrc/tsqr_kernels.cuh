@@ -932,18 +932,32 @@ __device__ __forceinline__ void apply_tile(unsigned char* apply_smem, T* tile, i
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
 
-        for (int idx = tid; idx < NMAX * NMAX; idx += NT) {
-            const int r = idx % NMAX, c = idx / NMAX;
-            const bool in = (r < ht && r < n && c < n);
-            const T v = in ? tile[r + c * p.ld] : T(0);
-            Vt[r][c] = (r > c) ? v : ((r == c && c < n) ? T(1) : T(0));
-            Tt[r][c] = (r <= c) ? v : T(0);
-            T b;
-            if (p.P)
-                b = (r < n && c < n) ? p.P[t * n + r + c * p.ldp] : T(0);
-            else
-                b = (r == c && r < n) ? T(1) : T(0);
-            Bs[r][c] = b;
+        {
+            // all global reads first: interleaved with the shared stores they
+            // would be issued one at a time (the generic pointers may alias)
+            constexpr int PER = (NMAX * NMAX + NT - 1) / NT;
+            T tv[PER], bv[PER];
+#pragma unroll
+            for (int e = 0; e < PER; ++e) {
+                const int idx = tid + NT * e;
+                const int r = idx % NMAX, c = idx / NMAX;
+                const bool ok = idx < NMAX * NMAX;
+                tv[e] = (ok && r < ht && r < n && c < n) ? tile[r + c * p.ld] : T(0);
+                if (p.P)
+                    bv[e] = (ok && r < n && c < n) ? p.P[t * n + r + c * p.ldp] : T(0);
+                else
+                    bv[e] = (r == c && r < n) ? T(1) : T(0);
+            }
+#pragma unroll
+            for (int e = 0; e < PER; ++e) {
+                const int idx = tid + NT * e;
+                const int r = idx % NMAX, c = idx / NMAX;
+                if (idx < NMAX * NMAX) {
+                    Vt[r][c] = (r > c) ? tv[e] : ((r == c && c < n) ? T(1) : T(0));
+                    Tt[r][c] = (r <= c) ? tv[e] : T(0);
+                    Bs[r][c] = bv[e];
+                }
+            }
         }
         __syncthreads();
         // Y = V_top^T B (V_top is unit lower triangular: terms r >= k)
