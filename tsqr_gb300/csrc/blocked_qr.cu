@@ -41,16 +41,30 @@ __global__ void __launch_bounds__(256) gemm_tn_partial(int M, int N, int64_t K, 
     const int64_t kbeg = (int64_t)blockIdx.z * kchunk;
     const int64_t kend = min(K, kbeg + kchunk);
     T acc[4][4] = {};
-    for (int64_t k0 = kbeg; k0 < kend; k0 += kKt) {
+    // the next k step's elements are loaded into registers while the current
+    // one is multiplied out of shared memory
+    T ra[4], rb[4];
+    auto fetch = [&](int64_t k0) {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             const int idx = tid + 256 * e;
             const int kk = idx % kKt, col = idx / kKt;
             const int64_t k = k0 + kk;
-            As[kk][col] = (k < kend && i0 + col < M) ? A[k + (int64_t)(i0 + col) * lda] : T(0);
-            Bs[kk][col] = (k < kend && j0 + col < N) ? B[k + (int64_t)(j0 + col) * ldb] : T(0);
+            ra[e] = (k < kend && i0 + col < M) ? A[k + (int64_t)(i0 + col) * lda] : T(0);
+            rb[e] = (k < kend && j0 + col < N) ? B[k + (int64_t)(j0 + col) * ldb] : T(0);
+        }
+    };
+    if (kbeg < kend) fetch(kbeg);
+    for (int64_t k0 = kbeg; k0 < kend; k0 += kKt) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int idx = tid + 256 * e;
+            const int kk = idx % kKt, col = idx / kKt;
+            As[kk][col] = ra[e];
+            Bs[kk][col] = rb[e];
         }
         __syncthreads();
+        if (k0 + kKt < kend) fetch(k0 + kKt);
 #pragma unroll
         for (int kk = 0; kk < kKt; ++kk) {
             T a[4], b[4];
@@ -102,22 +116,35 @@ __global__ void __launch_bounds__(256) gemm_nn(int64_t M, int N, int K, T alpha,
     const int64_t i0 = (int64_t)blockIdx.x * kTile;
     const int j0 = blockIdx.y * kTile;
     T acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += kKt) {
+    // the next k step's elements are loaded into registers while the current
+    // one is multiplied out of shared memory
+    T ra[4], rb[4];
+    auto fetch = [&](int k0) {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             const int idx = tid + 256 * e;
             {  // A tile: kKt columns of 64 contiguous rows
                 const int row = idx % kTile, kk = idx / kTile;
                 const int k = k0 + kk;
-                As[kk][row] = (k < K && i0 + row < M) ? A[i0 + row + (int64_t)k * lda] : T(0);
+                ra[e] = (k < K && i0 + row < M) ? A[i0 + row + (int64_t)k * lda] : T(0);
             }
             {  // B tile: 64 columns of kKt contiguous k
                 const int kk = idx % kKt, col = idx / kKt;
                 const int k = k0 + kk;
-                Bs[kk][col] = (k < K && j0 + col < N) ? B[k + (int64_t)(j0 + col) * ldb] : T(0);
+                rb[e] = (k < K && j0 + col < N) ? B[k + (int64_t)(j0 + col) * ldb] : T(0);
             }
         }
+    };
+    if (K > 0) fetch(0);
+    for (int k0 = 0; k0 < K; k0 += kKt) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int idx = tid + 256 * e;
+            As[(idx / kTile)][idx % kTile] = ra[e];
+            Bs[idx % kKt][idx / kKt] = rb[e];
+        }
         __syncthreads();
+        if (k0 + kKt < K) fetch(k0 + kKt);
 #pragma unroll
         for (int kk = 0; kk < kKt; ++kk) {
             T a[4], b[4];

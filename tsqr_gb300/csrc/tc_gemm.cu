@@ -86,7 +86,14 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
         // 8 rows of the same 16-byte K chunk (one 128-byte row of core
         // matrices: conflict-free stores) and 4 such groups cover 64
         // contiguous bytes of each row's column (full sectors).
-        for (int task = tid; task < 128 * (KS / 4); task += 128) {
+        // All global reads of a part are issued before its shared stores:
+        // interleaved, each iteration's loads would wait for the previous
+        // iteration's stores (the compiler cannot rule out aliasing).
+        constexpr int AT = 128 * (KS / 4) / 128;
+        float va[AT][4];
+#pragma unroll
+        for (int it = 0; it < AT; ++it) {
+            const int task = tid + 128 * it;
             int row, k4;
             if (TRANS_A) {
                 const int grp = task >> 5;
@@ -96,44 +103,71 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
                 row = task % 128;
                 k4 = (task / 128) * 4;
             }
-            float v[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const int64_t k = k0 + k4 + e;
                 const int m = m0 + row;
                 float x = 0.f;
                 if (k < kend && m < M) x = TRANS_A ? A[k + (int64_t)m * lda] : A[m + k * lda];
-                v[e] = x;
+                va[it][e] = x;
+            }
+        }
+#pragma unroll
+        for (int it = 0; it < AT; ++it) {
+            const int task = tid + 128 * it;
+            int row, k4;
+            if (TRANS_A) {
+                const int grp = task >> 5;
+                row = (grp % 16) * 8 + (task & 7);
+                k4 = ((grp / 16) * 4 + ((task >> 3) & 3)) * 4;
+            } else {
+                row = task % 128;
+                k4 = (task / 128) * 4;
             }
             uint4 hi, lo;
-            tc::split_tf32(v[0], hi.x, lo.x);
-            tc::split_tf32(v[1], hi.y, lo.y);
-            tc::split_tf32(v[2], hi.z, lo.z);
-            tc::split_tf32(v[3], hi.w, lo.w);
+            tc::split_tf32(va[it][0], hi.x, lo.x);
+            tc::split_tf32(va[it][1], hi.y, lo.y);
+            tc::split_tf32(va[it][2], hi.z, lo.z);
+            tc::split_tf32(va[it][3], hi.w, lo.w);
             const uint32_t off = tc::kmajor_off(row, k4, KS);
             *reinterpret_cast<uint4*>(ah + off) = hi;
             *reinterpret_cast<uint4*>(al + off) = lo;
         }
-        // B: NB rows (output columns) x KS; element (n, k) = Bm[k + n*ldb].
-        for (int task = tid; task < NB * (KS / 4); task += 128) {
-            const int grp = task >> 5;
-            const int row = (grp % (NB / 8)) * 8 + (task & 7);
-            const int k4 = ((grp / (NB / 8)) * 4 + ((task >> 3) & 3)) * 4;
-            float v[4];
+        // B: NB rows (output columns) x KS; element (n, k) = Bm[k + n*ldb],
+        // in rounds of at most 8 tasks per thread (loads, then stores).
+        constexpr int BT = NB * (KS / 4) / 128;
+        constexpr int BR = BT < 8 ? BT : 8;
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int64_t k = k0 + k4 + e;
-                const int nn = n0 + row;
-                v[e] = (k < kend && nn < N) ? Bm[k + (int64_t)nn * ldb] : 0.f;
+        for (int r0 = 0; r0 < BT; r0 += BR) {
+            float vb[BR][4];
+#pragma unroll
+            for (int it = 0; it < BR; ++it) {
+                const int task = tid + 128 * (r0 + it);
+                const int grp = task >> 5;
+                const int row = (grp % (NB / 8)) * 8 + (task & 7);
+                const int k4 = ((grp / (NB / 8)) * 4 + ((task >> 3) & 3)) * 4;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int64_t k = k0 + k4 + e;
+                    const int nn = n0 + row;
+                    vb[it][e] = (k < kend && nn < N) ? Bm[k + (int64_t)nn * ldb] : 0.f;
+                }
             }
-            uint4 hi, lo;
-            tc::split_tf32(v[0], hi.x, lo.x);
-            tc::split_tf32(v[1], hi.y, lo.y);
-            tc::split_tf32(v[2], hi.z, lo.z);
-            tc::split_tf32(v[3], hi.w, lo.w);
-            const uint32_t off = tc::kmajor_off(row, k4, KS);
-            *reinterpret_cast<uint4*>(bh + off) = hi;
-            *reinterpret_cast<uint4*>(bl + off) = lo;
+#pragma unroll
+            for (int it = 0; it < BR; ++it) {
+                const int task = tid + 128 * (r0 + it);
+                const int grp = task >> 5;
+                const int row = (grp % (NB / 8)) * 8 + (task & 7);
+                const int k4 = ((grp / (NB / 8)) * 4 + ((task >> 3) & 3)) * 4;
+                uint4 hi, lo;
+                tc::split_tf32(vb[it][0], hi.x, lo.x);
+                tc::split_tf32(vb[it][1], hi.y, lo.y);
+                tc::split_tf32(vb[it][2], hi.z, lo.z);
+                tc::split_tf32(vb[it][3], hi.w, lo.w);
+                const uint32_t off = tc::kmajor_off(row, k4, KS);
+                *reinterpret_cast<uint4*>(bh + off) = hi;
+                *reinterpret_cast<uint4*>(bl + off) = lo;
+            }
         }
         tc::fence_smem_to_async();
     };
