@@ -50,7 +50,18 @@ struct SplitCfg {
     static constexpr int ARPT = kRows / ANT;
     static_assert(kRows % ANT == 0, "apply block must divide the tile");
     static void factor(const FactorParams<T>& p, int grid, cudaStream_t s) {
-        factor_split_tiles<T, NMAX, CW, RPT, MINB><<<grid, 32 * (NMAX / CW), 0, s>>>(p);
+        // A single-tile level (the root) of h rows takes the same kernel with
+        // just enough rows per lane (32 * rpt >= h): every step issues the
+        // FMAs of all RPT rows of a lane, so a 64-row root on the 512-row
+        // kernel would spend 7/8 of them on zero rows.
+        constexpr int W32 = 32 * (NMAX / CW);
+        if constexpr (RPT > 2 && NMAX <= 64)
+            if (p.ntiles == 1 && p.h <= 64) return factor_split_tiles<T, NMAX, CW, 2, 1><<<1, W32, 0, s>>>(p);
+        if constexpr (RPT > 4)
+            if (p.ntiles == 1 && p.h <= 128) return factor_split_tiles<T, NMAX, CW, 4, 1><<<1, W32, 0, s>>>(p);
+        if constexpr (RPT > 8)
+            if (p.ntiles == 1 && p.h <= 256) return factor_split_tiles<T, NMAX, CW, 8, 1><<<1, W32, 0, s>>>(p);
+        factor_split_tiles<T, NMAX, CW, RPT, MINB><<<grid, W32, 0, s>>>(p);
     }
     static void apply(const ApplyParams<T>& p, int grid, cudaStream_t s) {
         TileCfg<T, NMAX, ANT, ARPT, 1, AMINB>::apply(p, grid, s);
