@@ -67,6 +67,26 @@ tsqr_status tsqr_s_ex(int64_t m, int64_t n, float* A, int64_t lda, float* R, int
 tsqr_status tsqr_d_ex(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr,
                       void* work, size_t work_bytes, const tsqr_opts* opts, void* stream);
 
+/* TSQR of a matrix in host memory, with Q and R returned to host memory:
+ * the call a program makes when its data are not on the GPU yet (the
+ * reference's driver copies A to the device before tsqr<T>,
+ * test_tsqr.cu:47-52).  Level 0 of the tree is cut into chunks of tiles; the
+ * host-to-device copy of each chunk overlaps the factorisation of the
+ * previous one, and the device-to-host copy of each chunk of Q overlaps the
+ * Q assembly of the next, on a copy stream of the call's own.  Use pinned host
+ * memory (cudaHostAlloc / cudaHostRegister) for the copies to overlap.
+ * A (m x n, lda) is only read; Q (m x n, ldq) and R (n x n, ldr) are written.
+ * work: device memory of tsqr_host_workspace_bytes bytes (a device copy of
+ * A and the tree).  Asynchronous: the results are complete when `stream`
+ * is.  precision PLAIN or TF32X3 (FP32 only). */
+size_t tsqr_host_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opts* opts);
+tsqr_status tsqr_s_host(int64_t m, int64_t n, const float* A, int64_t lda, float* Q, int64_t ldq,
+                        float* R, int64_t ldr, void* work, size_t work_bytes, const tsqr_opts* opts,
+                        void* stream);
+tsqr_status tsqr_d_host(int64_t m, int64_t n, const double* A, int64_t lda, double* Q, int64_t ldq,
+                        double* R, int64_t ldr, void* work, size_t work_bytes, const tsqr_opts* opts,
+                        void* stream);
+
 /* Recursive blocked QR: replaces qr<float>/qr<double> (block_QR.h:72-99):
  * qr(A1); R12 = A1^T A2; A2 -= A1 R12; qr(A2), TSQR panels at the leaves. */
 tsqr_status qr_s_ex(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr,

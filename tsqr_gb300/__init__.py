@@ -63,6 +63,11 @@ EXPORTS = {
     "tsqr_batched_s": ([ctypes.c_int, _p, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p],
                        ctypes.c_int),
     "tsqr_s_noalloc": ([_i64, _i64, _p, _i64, _p, _i64, _p], ctypes.c_int),
+    "tsqr_host_workspace_bytes": ([_i64, _i64, ctypes.c_int, ctypes.POINTER(Opts)], ctypes.c_size_t),
+    "tsqr_s_host": ([_i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p],
+                    ctypes.c_int),
+    "tsqr_d_host": ([_i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p],
+                    ctypes.c_int),
     "tsqr_profile": ([ctypes.c_int, ctypes.c_int, _i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t,
                       ctypes.POINTER(Opts), _p, _p, _p, ctypes.c_int, _p], ctypes.c_int),
     "tsqr_status_string": ([ctypes.c_int], ctypes.c_char_p),
@@ -202,6 +207,28 @@ def tsqr_(A, R=None, precision="plain", work=None, stream=None):
     _check(fn(m, n, A.data_ptr(), lda, R.data_ptr(), ldr, w.data_ptr(), wb, ctypes.byref(o),
               _stream_handle(stream)), "tsqr_")
     return R
+
+
+def tsqr_host_(A, Q=None, R=None, precision="plain", work=None, stream=None, device="cuda"):
+    """TSQR of the column-major m x n host (CPU) tensor A, pinned for the
+    copies to overlap: returns (Q, R) as host tensors (column-major).  The
+    transfers are pipelined with the level-0 kernels on the device."""
+    import torch
+    m, n = A.shape
+    lda = _ld(A)
+    if Q is None:
+        Q = torch.empty((n, m), dtype=A.dtype, pin_memory=A.is_pinned()).t()
+    if R is None:
+        R = torch.empty((n, n), dtype=A.dtype, pin_memory=A.is_pinned()).t()
+    o = _opts(precision)
+    nbytes = int(lib().tsqr_host_workspace_bytes(m, n, A.element_size(), ctypes.byref(o)))
+    if nbytes == 0:
+        raise TsqrError(2, "tsqr_host_ workspace (m=%d n=%d)" % (m, n))
+    w, wb = _work(nbytes, work, torch.device(device))
+    fn = lib().tsqr_s_host if A.dtype == torch.float32 else lib().tsqr_d_host
+    _check(fn(m, n, A.data_ptr(), lda, Q.data_ptr(), _ld(Q), R.data_ptr(), _ld(R), w.data_ptr(), wb,
+              ctypes.byref(o), _stream_handle(stream)), "tsqr_host_")
+    return Q, R
 
 
 def qr_(A, R=None, precision="plain", reorth=False, panel=0, work=None, stream=None):

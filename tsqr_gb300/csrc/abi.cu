@@ -80,6 +80,20 @@ tsqr_status ref_form(int m, int n, T* A, int lda, T* R, int ldr, T* d_work, int 
               : tsqr_ex<T>(m, n, A, lda, R, ldr, work, have, &o, nullptr);
 }
 
+template <typename T>
+tsqr_status tsqr_host_call(int64_t m, int64_t n, const T* A, int64_t lda, T* Q, int64_t ldq, T* R, int64_t ldr,
+                           void* work, size_t work_bytes, const tsqr_opts* op, void* stream) {
+    const tsqr_opts o = opts_or_default(op);
+    tsqr_status st = check_common<T>(m, n, A, lda, R, ldr, o);
+    if (st != TSQR_OK) return st;
+    if (Q == nullptr || ldq < m) return TSQR_ERR_INVALID_ARG;
+    if (n > max_tsqr_n<T>()) return TSQR_ERR_UNSUPPORTED;
+    if (o.precision == TSQR_PRECISION_BF16X3 || (sizeof(T) == 8 && o.precision != TSQR_PRECISION_PLAIN))
+        return TSQR_ERR_UNSUPPORTED;
+    return tsqr::tsqr_host<T>(m, n, A, lda, Q, ldq, R, ldr, work, work_bytes,
+                              o.precision == TSQR_PRECISION_TF32X3, (cudaStream_t)stream);
+}
+
 }  // namespace
 
 extern "C" {
@@ -92,6 +106,24 @@ size_t tsqr_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opt
     if (elem_bytes == 4) return n <= 64 ? tsqr::tsqr_plain_workspace<float>(m, n) : 0;
     if (elem_bytes == 8) return n <= 32 ? tsqr::tsqr_plain_workspace<double>(m, n) : 0;
     return 0;
+}
+
+size_t tsqr_host_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opts* opts) {
+    const tsqr_opts o = opts_or_default(opts);
+    if (m < 1 || n < 1 || m < n) return 0;
+    const bool prec = o.precision == TSQR_PRECISION_TF32X3;
+    if (elem_bytes == 4) return n <= 64 ? tsqr::tsqr_host_workspace<float>(m, n, prec) : 0;
+    if (elem_bytes == 8) return (n <= 32 && !prec) ? tsqr::tsqr_host_workspace<double>(m, n, false) : 0;
+    return 0;
+}
+
+tsqr_status tsqr_s_host(int64_t m, int64_t n, const float* A, int64_t lda, float* Q, int64_t ldq, float* R,
+                        int64_t ldr, void* work, size_t work_bytes, const tsqr_opts* opts, void* stream) {
+    return tsqr_host_call<float>(m, n, A, lda, Q, ldq, R, ldr, work, work_bytes, opts, stream);
+}
+tsqr_status tsqr_d_host(int64_t m, int64_t n, const double* A, int64_t lda, double* Q, int64_t ldq, double* R,
+                        int64_t ldr, void* work, size_t work_bytes, const tsqr_opts* opts, void* stream) {
+    return tsqr_host_call<double>(m, n, A, lda, Q, ldq, R, ldr, work, work_bytes, opts, stream);
 }
 
 size_t qr_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opts* opts) {

@@ -50,6 +50,13 @@ void* cached_workspace(size_t bytes, tsqr_status* st);
 namespace tsqr {
 // Precision form of TSQR (tsqr.cu + tc_apply.cu), FP32 only.
 size_t tsqr_precision_workspace(int64_t m, int64_t n);
+// TSQR of host-resident A with host Q and R, transfers pipelined with the
+// level-0 kernels (tsqr.cu).  prec: the precision form (FP32 only).
+template <typename T>
+size_t tsqr_host_workspace(int64_t m, int64_t n, bool prec);
+template <typename T>
+tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int64_t ldq, T* hR, int64_t ldr,
+                      void* work, size_t work_bytes, bool prec, cudaStream_t s);
 tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
                            size_t work_bytes, cudaStream_t s);
 }  // namespace tsqr

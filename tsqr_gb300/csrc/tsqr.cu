@@ -356,6 +356,195 @@ template tsqr_status tsqr_plain<double>(int64_t, int64_t, double*, int64_t, doub
                                         cudaStream_t);
 
 // ---------------------------------------------------------------------------
+// TSQR of a matrix in host memory (tsqr_s_host / tsqr_d_host).  The device
+// holds a copy of A (ld rounded up to 32 rows), the n x n R and the tree.
+// Level 0 is cut into chunks of whole tiles.  A library copy stream moves
+// chunk c to the device while the caller's stream factors chunk c-1; after
+// the upper levels, the caller's stream assembles Q chunk by chunk while the
+// copy stream returns the finished chunks, so both host transfers overlap
+// the level-0 kernels instead of adding to them.  Streams and events are
+// made per call (no shared state between calls); the runtime releases them
+// once the work that uses them has completed.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kHostChunks = 8;
+
+template <typename T>
+struct HostLayout {
+    int64_t ldd = 0;
+    size_t a = 0, r = 0, tree = 0, total = 0;
+};
+
+template <typename T>
+HostLayout<T> host_layout(int64_t m, int64_t n, bool prec) {
+    HostLayout<T> L;
+    L.ldd = round_up(m, 32);
+    L.a = 0;
+    L.r = (size_t)round_up(L.ldd * n * (int64_t)sizeof(T), (int64_t)kAlign);
+    L.tree = L.r + (size_t)round_up(n * n * (int64_t)sizeof(T), (int64_t)kAlign);
+    size_t tw = 0;
+    if constexpr (sizeof(T) == 4) {
+        if (prec) {
+            PrecCfg c = pick_precision((int)n);
+            tw = c.ks.factor ? prec_layout(m, n, c).total : 0;
+        }
+    }
+    if (!prec) tw = tsqr_plain_workspace<T>(m, n);
+    L.total = tw ? L.tree + tw : 0;
+    return L;
+}
+
+}  // namespace
+
+template <typename T>
+size_t tsqr_host_workspace(int64_t m, int64_t n, bool prec) {
+    return host_layout<T>(m, n, prec).total;
+}
+
+template <typename T>
+tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int64_t ldq, T* hR, int64_t ldr,
+                      void* work, size_t work_bytes, bool prec, cudaStream_t s) {
+    const HostLayout<T> HL = host_layout<T>(m, n, prec);
+    if (HL.total == 0) return TSQR_ERR_UNSUPPORTED;
+    if (work == nullptr || work_bytes < HL.total) return TSQR_ERR_WORKSPACE;
+    char* base = reinterpret_cast<char*>(work);
+    T* dA = reinterpret_cast<T*>(base + HL.a);
+    T* dR = reinterpret_cast<T*>(base + HL.r);
+    char* tw = base + HL.tree;
+    const size_t twb = work_bytes - HL.tree;
+
+    // the tree of the chosen form
+    KernelSet<T> ks;
+    int nmax = 0;
+    bool tc = false;
+    int* err = nullptr;
+    char* lvbase = tw;
+    if constexpr (sizeof(T) == 4) {
+        if (prec) {
+            PrecCfg c = pick_precision((int)n);
+            const PrecLayout PL = prec_layout(m, n, c);
+            ks = c.ks;
+            nmax = c.nmax;
+            tc = c.nmax <= 32;
+            err = reinterpret_cast<int*>(tw + PL.status);
+            lvbase = tw + PL.levels;
+        }
+    }
+    if (!prec) ks = pick((T*)nullptr, (int)n);
+    if (!ks.factor) return TSQR_ERR_UNSUPPORTED;
+    (void)twb;
+    std::vector<Level<T>> lv;
+    plan_levels<T>(m, n, dA, HL.ldd, ks.rows, lvbase, &lv);
+    const int L = (int)lv.size();
+    const int64_t rows = ks.rows;
+
+    auto factor = [&](int l, int64_t t0, int64_t cnt) {
+        FactorParams<T> fp;
+        fp.M = lv[l].M + t0 * rows;
+        fp.ld = lv[l].ld;
+        fp.h = std::min<int64_t>(cnt * rows, lv[l].h - t0 * rows);
+        fp.n = (int)n;
+        fp.ntiles = cnt;
+        fp.Rout = (l == L - 1) ? dR : lv[l + 1].M + t0 * n;
+        fp.ldr = (l == L - 1) ? n : lv[l + 1].ld;
+        ks.factor(fp, (int)std::min<int64_t>(cnt, 1 << 30), s);
+        log_launch(kTagFactor + l, s);
+    };
+    auto apply = [&](int l, int64_t t0, int64_t cnt) -> bool {
+        ApplyParams<T> ap;
+        ap.M = lv[l].M + t0 * rows;
+        ap.ld = lv[l].ld;
+        ap.h = std::min<int64_t>(cnt * rows, lv[l].h - t0 * rows);
+        ap.n = (int)n;
+        ap.ntiles = cnt;
+        ap.P = (l == L - 1) ? nullptr : lv[l + 1].M + t0 * n;
+        ap.ldp = (l == L - 1) ? 0 : lv[l + 1].ld;
+        if constexpr (sizeof(T) == 4) {
+            if (tc) {
+                ap.vec = 0;
+                if (!tc_apply_level(ap, nmax, (int)rows, err, s)) return false;
+                log_launch(kTagTc + l, s);
+                return true;
+            }
+        }
+        constexpr int ve = 16 / sizeof(T);
+        ap.vec = (ap.ld % ve == 0 && (reinterpret_cast<uintptr_t>(ap.M) % 16) == 0) ? 1 : 0;
+        ks.apply(ap, (int)std::min<int64_t>(cnt, 1 << 30), s);
+        log_launch(kTagApply + l, s);
+        return true;
+    };
+
+    // per-call copy stream and events
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return TSQR_ERR_CUDA;
+    cudaEvent_t ev[2 * kHostChunks + 2];
+    int nev = 0;
+    tsqr_status st = TSQR_OK;
+    for (; nev < 2 * kHostChunks + 2; ++nev)
+        if (cudaEventCreateWithFlags(&ev[nev], cudaEventDisableTiming) != cudaSuccess) {
+            st = TSQR_ERR_CUDA;
+            break;
+        }
+    const int64_t nt0 = lv[0].ntiles;
+    const int nc = (int)std::min<int64_t>(kHostChunks, nt0);
+    const int64_t per = ceil_div(nt0, nc);
+    const size_t es = sizeof(T);
+    if (st == TSQR_OK) {
+        // the copy stream starts after the caller's earlier work
+        cudaEventRecord(ev[2 * kHostChunks], s);
+        cudaStreamWaitEvent(cs, ev[2 * kHostChunks], 0);
+        if (err) cudaMemsetAsync(err, 0, sizeof(int), s);
+        // up: chunk c copied in while chunk c-1 is factored
+        for (int c = 0; c < nc; ++c) {
+            const int64_t t0 = c * per, cnt = std::min<int64_t>(per, nt0 - t0);
+            if (cnt <= 0) break;
+            const int64_t r0 = t0 * rows, hr = std::min<int64_t>(cnt * rows, m - r0);
+            if (cudaMemcpy2DAsync(dA + r0, HL.ldd * es, hA + r0, lda * es, hr * es, n, cudaMemcpyHostToDevice, cs) !=
+                cudaSuccess)
+                st = TSQR_ERR_CUDA;
+            cudaEventRecord(ev[c], cs);
+            cudaStreamWaitEvent(s, ev[c], 0);
+            factor(0, t0, cnt);
+        }
+        for (int l = 1; l < L; ++l) factor(l, 0, lv[l].ntiles);
+        for (int l = L - 1; l >= 1 && st == TSQR_OK; --l)
+            if (!apply(l, 0, lv[l].ntiles)) st = TSQR_ERR_UNSUPPORTED;
+        if (cudaMemcpy2DAsync(hR, ldr * es, dR, n * es, n * es, n, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            st = TSQR_ERR_CUDA;
+        // down: chunk c of Q returned while chunk c+1 is assembled
+        for (int c = 0; c < nc && st == TSQR_OK; ++c) {
+            const int64_t t0 = c * per, cnt = std::min<int64_t>(per, nt0 - t0);
+            if (cnt <= 0) break;
+            const int64_t r0 = t0 * rows, hr = std::min<int64_t>(cnt * rows, m - r0);
+            if (!apply(0, t0, cnt)) {
+                st = TSQR_ERR_UNSUPPORTED;
+                break;
+            }
+            cudaEventRecord(ev[kHostChunks + c], s);
+            cudaStreamWaitEvent(cs, ev[kHostChunks + c], 0);
+            if (cudaMemcpy2DAsync(hQ + r0, ldq * es, dA + r0, HL.ldd * es, hr * es, n, cudaMemcpyDeviceToHost, cs) !=
+                cudaSuccess)
+                st = TSQR_ERR_CUDA;
+        }
+        // the caller's stream completes after the last copy
+        cudaEventRecord(ev[2 * kHostChunks + 1], cs);
+        cudaStreamWaitEvent(s, ev[2 * kHostChunks + 1], 0);
+    }
+    for (int i = 0; i < nev; ++i) cudaEventDestroy(ev[i]);
+    cudaStreamDestroy(cs);
+    if (st != TSQR_OK) return st;
+    return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
+}
+
+template size_t tsqr_host_workspace<float>(int64_t, int64_t, bool);
+template size_t tsqr_host_workspace<double>(int64_t, int64_t, bool);
+template tsqr_status tsqr_host<float>(int64_t, int64_t, const float*, int64_t, float*, int64_t, float*, int64_t,
+                                      void*, size_t, bool, cudaStream_t);
+template tsqr_status tsqr_host<double>(int64_t, int64_t, const double*, int64_t, double*, int64_t, double*,
+                                       int64_t, void*, size_t, bool, cudaStream_t);
+
+// ---------------------------------------------------------------------------
 // Per-device workspace cache for the reference-signature entry points, whose
 // d_work is sized for the reference's own layout (ldwork*n elements with
 // ldwork = 2*NUM_SM*BLOCK_SIZE, test_tsqr.cu:42-45).
