@@ -130,3 +130,33 @@ def test_blocked_qr_precision_large_kappa(cuda, tg):
     u = 2.0 ** -24
     for back, orth in figs.values():
         assert back <= 1e-5 and orth <= 10 * n * u, figs
+
+
+def test_workspace_status_word_is_clear_after_tensor_core_calls(orc, cuda, tg):
+    """The tcgen05 kernels' bounded mbarrier waits report a timeout through
+    the status word at the start of the workspace; after ordinary calls of
+    every precision-form entry point it must read clear."""
+    import torch
+    m, n = 70000, 32
+    A = orc.fill_uniform(m, n, np.float32, seed=9)
+    dA = to_dev(tg, A)
+    nb = tg.workspace_bytes(m, n, torch.float32, precision="tf32x3")
+    w = torch.full((nb,), 0xFF, dtype=torch.uint8, device="cuda")  # the call must clear the word itself
+    tg.tsqr_(dA, precision="tf32x3", work=w)
+    torch.cuda.synchronize()
+    assert tg.lib().tsqr_workspace_check(w.data_ptr()) == 0
+    m2, n2 = 20000, 256
+    B = to_dev(tg, orc.fill_uniform(m2, n2, np.float32, seed=10))
+    nb2 = tg.qr_workspace_bytes(m2, n2, torch.float32, precision="tf32x3")
+    w2 = torch.full((nb2,), 0xFF, dtype=torch.uint8, device="cuda")
+    tg.qr_(B, precision="tf32x3", work=w2)
+    torch.cuda.synchronize()
+    assert tg.lib().tsqr_workspace_check(w2.data_ptr()) == 0
+    hA = torch.from_numpy(np.ascontiguousarray(A.T)).pin_memory().t()
+    o = tg._opts("tf32x3")
+    import ctypes
+    nb3 = int(tg.lib().tsqr_host_workspace_bytes(m, n, 4, ctypes.byref(o)))
+    w3 = torch.full((nb3,), 0xFF, dtype=torch.uint8, device="cuda")
+    tg.tsqr_host_(hA, precision="tf32x3", work=w3)
+    torch.cuda.synchronize()
+    assert tg.lib().tsqr_workspace_check(w3.data_ptr()) == 0

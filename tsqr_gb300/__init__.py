@@ -64,6 +64,7 @@ EXPORTS = {
                        ctypes.c_int),
     "tsqr_s_noalloc": ([_i64, _i64, _p, _i64, _p, _i64, _p], ctypes.c_int),
     "tsqr_host_workspace_bytes": ([_i64, _i64, ctypes.c_int, ctypes.POINTER(Opts)], ctypes.c_size_t),
+    "tsqr_workspace_check": ([_p], ctypes.c_int),
     "tsqr_s_host": ([_i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p],
                     ctypes.c_int),
     "tsqr_d_host": ([_i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p],

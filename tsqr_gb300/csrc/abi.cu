@@ -108,6 +108,13 @@ size_t tsqr_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opt
     return 0;
 }
 
+tsqr_status tsqr_workspace_check(const void* work) {
+    if (work == nullptr) return TSQR_ERR_INVALID_ARG;
+    int word = 0;
+    if (cudaMemcpy(&word, work, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return TSQR_ERR_CUDA;
+    return word == 0 ? TSQR_OK : TSQR_ERR_CUDA;
+}
+
 size_t tsqr_host_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opts* opts) {
     const tsqr_opts o = opts_or_default(opts);
     if (m < 1 || n < 1 || m < n) return 0;

@@ -376,13 +376,12 @@ struct HostLayout {
     size_t a = 0, r = 0, tree = 0, total = 0;
 };
 
+// The tree comes first, so the precision form's status word sits at the
+// start of the workspace as for the device entry points.
 template <typename T>
 HostLayout<T> host_layout(int64_t m, int64_t n, bool prec) {
     HostLayout<T> L;
     L.ldd = round_up(m, 32);
-    L.a = 0;
-    L.r = (size_t)round_up(L.ldd * n * (int64_t)sizeof(T), (int64_t)kAlign);
-    L.tree = L.r + (size_t)round_up(n * n * (int64_t)sizeof(T), (int64_t)kAlign);
     size_t tw = 0;
     if constexpr (sizeof(T) == 4) {
         if (prec) {
@@ -391,7 +390,11 @@ HostLayout<T> host_layout(int64_t m, int64_t n, bool prec) {
         }
     }
     if (!prec) tw = tsqr_plain_workspace<T>(m, n);
-    L.total = tw ? L.tree + tw : 0;
+    L.tree = 0;
+    L.a = (size_t)round_up((int64_t)tw, (int64_t)kAlign);
+    L.r = L.a + (size_t)round_up(L.ldd * n * (int64_t)sizeof(T), (int64_t)kAlign);
+    const size_t end = L.r + (size_t)round_up(n * n * (int64_t)sizeof(T), (int64_t)kAlign);
+    L.total = tw ? end : 0;
     return L;
 }
 
@@ -412,7 +415,6 @@ tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int
     T* dA = reinterpret_cast<T*>(base + HL.a);
     T* dR = reinterpret_cast<T*>(base + HL.r);
     char* tw = base + HL.tree;
-    const size_t twb = work_bytes - HL.tree;
 
     // the tree of the chosen form
     KernelSet<T> ks;
@@ -433,7 +435,6 @@ tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int
     }
     if (!prec) ks = pick((T*)nullptr, (int)n);
     if (!ks.factor) return TSQR_ERR_UNSUPPORTED;
-    (void)twb;
     std::vector<Level<T>> lv;
     plan_levels<T>(m, n, dA, HL.ldd, ks.rows, lvbase, &lv);
     const int L = (int)lv.size();
