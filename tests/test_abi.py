@@ -82,3 +82,29 @@ def test_workspace_sizes_are_small(tg):
     assert tg.workspace_bytes(100, 200, "float32") == 0        # m < n
     assert tg.qr_workspace_bytes(27648, 128, "float64") > 0
     assert tg.qr_workspace_bytes(27648, 128, "float64", reorth=True) > tg.qr_workspace_bytes(27648, 128, "float64")
+
+
+def test_host_entry_argument_checks_need_no_gpu(tg):
+    """tsqr_s_host / tsqr_d_host reject bad sizes, leading dimensions,
+    options and workspaces before any CUDA call."""
+    L = tg.lib()
+    a = (ctypes.c_float * 400)()
+    q = (ctypes.c_float * 400)()
+    r = (ctypes.c_float * 16)()
+    o = tg._opts("plain")
+    p = lambda x: ctypes.cast(x, ctypes.c_void_p)
+
+    def call(m, n, lda, ldq, ldr, work=1, nbytes=1 << 30, opts=o, fn=L.tsqr_s_host):
+        return fn(m, n, p(a), lda, p(q), ldq, p(r), ldr, ctypes.c_void_p(work), nbytes, ctypes.byref(opts), None)
+
+    assert call(100, 4, 99, 100, 4) == 1    # lda < m
+    assert call(100, 4, 100, 99, 4) == 1    # ldq < m
+    assert call(100, 4, 100, 100, 3) == 1   # ldr < n
+    assert call(3, 4, 100, 100, 4) == 1     # m < n
+    assert call(100, 65, 100, 100, 65) == 2  # n above the FP32 limit
+    assert call(100, 4, 100, 100, 4, work=0) == 3
+    assert call(100, 4, 100, 100, 4, nbytes=16) == 3
+    assert call(100, 4, 100, 100, 4, opts=tg._opts("bf16x3")) == 2
+    assert call(100, 4, 100, 100, 4, opts=tg._opts("tf32x3"), fn=L.tsqr_d_host) == 2
+    assert L.tsqr_host_workspace_bytes(100, 4, 4, ctypes.byref(o)) > 100 * 4 * 4
+    assert L.tsqr_host_workspace_bytes(3, 4, 4, ctypes.byref(o)) == 0
