@@ -362,13 +362,39 @@ template tsqr_status tsqr_plain<double>(int64_t, int64_t, double*, int64_t, doub
 // chunk c to the device while the caller's stream factors chunk c-1; after
 // the upper levels, the caller's stream assembles Q chunk by chunk while the
 // copy stream returns the finished chunks, so both host transfers overlap
-// the level-0 kernels instead of adding to them.  Streams and events are
-// made per call (no shared state between calls); the runtime releases them
-// once the work that uses them has completed.
+// the level-0 kernels instead of adding to them.  The copy stream and its
+// events belong to the calling host thread (one set per device), so calls
+// from different threads share nothing; a problem of one chunk copies on
+// the caller's stream alone.
 // ---------------------------------------------------------------------------
 namespace {
 
 constexpr int kHostChunks = 8;
+constexpr int64_t kHostChunkBytes = 16 << 20;
+
+// Copy stream and events of one host thread on one device.
+struct HostPipe {
+    int dev = -1;
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev[2 * kHostChunks + 2] = {};
+};
+
+HostPipe* host_pipe() {
+    thread_local HostPipe pipes[8];
+    thread_local int used = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    for (int i = 0; i < used; ++i)
+        if (pipes[i].dev == dev) return &pipes[i];
+    if (used == 8) return nullptr;
+    HostPipe& p = pipes[used];
+    if (cudaStreamCreateWithFlags(&p.cs, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    for (auto& e : p.ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    p.dev = dev;
+    ++used;
+    return &p;
+}
 
 template <typename T>
 struct HostLayout {
@@ -476,22 +502,41 @@ tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int
         return true;
     };
 
-    // per-call copy stream and events
-    cudaStream_t cs = nullptr;
-    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return TSQR_ERR_CUDA;
-    cudaEvent_t ev[2 * kHostChunks + 2];
-    int nev = 0;
-    tsqr_status st = TSQR_OK;
-    for (; nev < 2 * kHostChunks + 2; ++nev)
-        if (cudaEventCreateWithFlags(&ev[nev], cudaEventDisableTiming) != cudaSuccess) {
-            st = TSQR_ERR_CUDA;
-            break;
-        }
     const int64_t nt0 = lv[0].ntiles;
-    const int nc = (int)std::min<int64_t>(kHostChunks, nt0);
+    // chunks of at least kHostChunkBytes: smaller copies gain less from the
+    // overlap than the extra launches and stream operations cost
+    const int64_t by_size = std::max<int64_t>(1, (m * n * (int64_t)sizeof(T)) / kHostChunkBytes);
+    const int nc = (int)std::min<int64_t>(std::min<int64_t>(kHostChunks, nt0), by_size);
     const int64_t per = ceil_div(nt0, nc);
     const size_t es = sizeof(T);
-    if (st == TSQR_OK) {
+    tsqr_status st = TSQR_OK;
+    // One chunk leaves nothing to overlap: copies on the caller's stream.
+    // Otherwise the copy stream and events of this host thread (made once per
+    // thread and device, reused by its later calls: a host thread issues its
+    // calls one after another, and a wait captures an event's state when it
+    // is enqueued, so re-recording an event cannot disturb an earlier call).
+    cudaStream_t cs = s;
+    cudaEvent_t* ev = nullptr;
+    if (nc > 1) {
+        HostPipe* hp = host_pipe();
+        if (!hp) return TSQR_ERR_CUDA;
+        cs = hp->cs;
+        ev = hp->ev;
+    }
+    if (nc == 1) {
+        const int64_t hr = m;
+        if (cudaMemcpy2DAsync(dA, HL.ldd * es, hA, lda * es, hr * es, n, cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return TSQR_ERR_CUDA;
+        if (err) cudaMemsetAsync(err, 0, sizeof(int), s);
+        for (int l = 0; l < L; ++l) factor(l, 0, lv[l].ntiles);
+        for (int l = L - 1; l >= 0; --l)
+            if (!apply(l, 0, lv[l].ntiles)) return TSQR_ERR_UNSUPPORTED;
+        if (cudaMemcpy2DAsync(hR, ldr * es, dR, n * es, n * es, n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpy2DAsync(hQ, ldq * es, dA, HL.ldd * es, hr * es, n, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return TSQR_ERR_CUDA;
+        return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
+    }
+    {
         // the copy stream starts after the caller's earlier work
         cudaEventRecord(ev[2 * kHostChunks], s);
         cudaStreamWaitEvent(cs, ev[2 * kHostChunks], 0);
@@ -532,8 +577,6 @@ tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int
         cudaEventRecord(ev[2 * kHostChunks + 1], cs);
         cudaStreamWaitEvent(s, ev[2 * kHostChunks + 1], 0);
     }
-    for (int i = 0; i < nev; ++i) cudaEventDestroy(ev[i]);
-    cudaStreamDestroy(cs);
     if (st != TSQR_OK) return st;
     return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
 }
