@@ -566,6 +566,28 @@ __device__ __forceinline__ double fmadd(double a, double b, double c) { return f
 __device__ __forceinline__ float sqrt_t(float x) { return sqrtf(x); }
 __device__ __forceinline__ double sqrt_t(double x) { return sqrt(x); }
 
+// Reflector scalars on the owner's critical chain, FP32, branch-free: the
+// hardware approximations refined by Newton-Raphson and finished with one
+// residual correction each.  sqrt: r ~ 1/sqrt(x), r <- r (3 - x r^2) / 2,
+// s = x r, s <- s + (r/2)(x - s^2) with the residual by FMA; reciprocal:
+// r <- r (2 - x r), r <- r + r (1 - x r).  Both land within rounding of the
+// correctly rounded results without the slow-path branches of the IEEE
+// sequences.  Only used for x > 0 (the zero-column case selects other
+// values).  FP64 keeps the exact operations.
+__device__ __forceinline__ float refl_sqrt(float x) {
+    float r = rsqrtf(x);
+    r = r * fmaf(-0.5f * x * r, r, 1.5f);
+    const float s = x * r;
+    return fmaf(0.5f * r, fmaf(-s, s, x), s);
+}
+__device__ __forceinline__ double refl_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float refl_recip(float x) {
+    float r = __fdividef(1.0f, x);
+    r = r * fmaf(-x, r, 2.0f);
+    return fmaf(r, fmaf(-x, r, 1.0f), r);
+}
+__device__ __forceinline__ double refl_recip(double x) { return 1.0 / x; }
+
 // 16-byte vector of T.
 template <typename T>
 struct Vec16;
@@ -705,10 +727,10 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
                 for (int u = 0; u < U; ++u) {
                     const int j = pc0 + base + u;
                     const bool zero = (sig2 == T(0));
-                    const T nrm = sqrt_t(fmadd(alpha, alpha, sig2));
+                    const T nrm = refl_sqrt(fmadd(alpha, alpha, sig2));
                     const T beta = zero ? alpha : ((alpha >= T(0)) ? -nrm : nrm);
-                    const T tau = zero ? T(0) : (beta - alpha) * recip(beta);
-                    const T scale = zero ? T(0) : recip(alpha - beta);
+                    const T tau = zero ? T(0) : (beta - alpha) * refl_recip(beta);
+                    const T scale = zero ? T(0) : refl_recip(alpha - beta);
 #pragma unroll
                     for (int i = 0; i < RPT; ++i)
                         if (below(i, j)) y[i][u] *= scale;
