@@ -567,8 +567,8 @@ __device__ __forceinline__ float sqrt_t(float x) { return sqrtf(x); }
 __device__ __forceinline__ double sqrt_t(double x) { return sqrt(x); }
 
 // Reflector scalars on the owner's critical chain, FP32, branch-free: the
-// hardware approximations refined by Newton-Raphson and finished with one
-// residual correction each.  sqrt: r ~ 1/sqrt(x), r <- r (3 - x r^2) / 2,
+// hardware approximations refined by a Newton-Raphson step and finished with
+// one residual correction each (Markstein's method for sqrt and reciprocal).  sqrt: r ~ 1/sqrt(x), r <- r (3 - x r^2) / 2,
 // s = x r, s <- s + (r/2)(x - s^2) with the residual by FMA; reciprocal:
 // r <- r (2 - x r), r <- r + r (1 - x r).  Both land within rounding of the
 // correctly rounded results without the slow-path branches of the IEEE
