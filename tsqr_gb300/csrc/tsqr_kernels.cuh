@@ -711,12 +711,12 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
             // next column reduced while the current update is issued
             T sig2, alpha;
             {
-                T s = 0;
+                T s4[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
                 for (int i = 0; i < RPT; ++i)
-                    if (below(i, pc0)) s = fmadd(y[i][0], y[i][0], s);
+                    if (below(i, pc0)) s4[i & 3] = fmadd(y[i][0], y[i][0], s4[i & 3]);
                 alpha = __shfl_sync(kFull, diag_slot(y, 0, pc0), pc0 & 31);
-                sig2 = warp_sum(s);
+                sig2 = warp_sum((s4[0] + s4[1]) + (s4[2] + s4[3]));
             }
 #pragma unroll 1
             for (int g = 0; g < G; ++g) {
@@ -773,12 +773,12 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
                         const int c = (u + 1 < CW) ? u + 1 : 0;  // keeps the index in range when u + 1 == CW
 #pragma unroll
                         for (int i = 0; i < RPT; ++i) y[i][c] = fmadd(-tv[i], cf[c], y[i][c]);
-                        T s = 0;
+                        T s4[4] = {T(0), T(0), T(0), T(0)};  // four chains instead of one RPT-deep one
 #pragma unroll
                         for (int i = 0; i < RPT; ++i)
-                            if (below(i, j + 1)) s = fmadd(y[i][c], y[i][c], s);
+                            if (below(i, j + 1)) s4[i & 3] = fmadd(y[i][c], y[i][c], s4[i & 3]);
                         alpha = __shfl_sync(kFull, diag_slot(y, c, j + 1), (j + 1) & 31);
-                        sig2 = warp_sum(s);
+                        sig2 = warp_sum((s4[0] + s4[1]) + (s4[2] + s4[3]));
                     }
 #pragma unroll
                     for (int c = u + 2; c < CW; ++c)
