@@ -619,6 +619,44 @@ __host__ __device__ constexpr int colsum_stride() {
     return (sizeof(T) == 4 && CW == 4) ? 4 : CW + 16 / (int)sizeof(T);
 }
 
+// Layout of the published reflector: lane-major in 16-byte chunks when RPT
+// allows (KC = RPT / VN chunks per lane, a power of two up to 8), so a lane moves its
+// RPT values with KC vector accesses; chunk k of lane l sits at chunk
+// position k ^ ((l / (8 / KC)) & (KC - 1)) of the lane's row, which puts the
+// 8 lanes of each 16-byte access phase on 8 distinct 4-bank groups.
+// Otherwise slot i of lane l is element l + 32 i (scalar accesses).
+template <typename T, int RPT>
+struct VbufLayout {
+    static constexpr int VN = Vec16<T>::N;
+    static constexpr int KC = RPT / VN;
+    static constexpr bool kVec = (RPT % VN == 0) && KC >= 1 && KC <= 8 && (KC & (KC - 1)) == 0;
+    __device__ static int swz(int lane) { return kVec ? (lane / (8 / KC)) & (KC - 1) : 0; }
+    template <typename F>
+    __device__ static void store(T* buf, int lane, int sw, F&& val) {
+        if constexpr (kVec) {
+#pragma unroll
+            for (int k = 0; k < KC; ++k) {
+                T t[VN];
+#pragma unroll
+                for (int e = 0; e < VN; ++e) t[e] = val(k * VN + e);
+                Vec16<T>::store(buf + lane * RPT + VN * (k ^ sw), t);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) buf[lane + 32 * i] = val(i);
+        }
+    }
+    __device__ static void load(const T* buf, int lane, int sw, T (&v)[RPT]) {
+        if constexpr (kVec) {
+#pragma unroll
+            for (int k = 0; k < KC; ++k) Vec16<T>::load(buf + lane * RPT + VN * (k ^ sw), &v[k * VN]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) v[i] = buf[lane + 32 * i];
+        }
+    }
+};
+
 template <typename T, int NMAX, int CW, int RPT>
 struct SplitFactorSmem {
     static constexpr int W = NMAX / CW;
@@ -678,6 +716,7 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
     const int col0 = warp * CW;
     const int mycols = max(0, min(CW, n - col0));
     T* scratch = S.xpose[warp];
+    const int vsw = VbufLayout<T, RPT>::swz(lane);
     // Row lane + 32*i lies strictly below diagonal element j (compile-time
     // true for every slot i >= 1 when NMAX <= 32).
     auto below = [&](int i, int j) { return (NMAX <= 32 && i > 0) || (lane + 32 * i > j); };
@@ -737,8 +776,7 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
                     // v_j of slot i (1 on the diagonal, 0 above it)
                     auto vj = [&](int i) { return below(i, j) ? y[i][u] : ((lane + 32 * i == j) ? T(1) : T(0)); };
                     const int b = j & 1;
-#pragma unroll
-                    for (int i = 0; i < RPT; ++i) S.vbuf[b][lane + 32 * i] = vj(i);
+                    VbufLayout<T, RPT>::store(S.vbuf[b], lane, vsw, vj);
                     if (lane == 0) {
                         S.taub[b] = tau;
                         S.tau[j] = tau;
@@ -807,8 +845,7 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
                 step_barrier(W * 32);
                 const int b = j & 1;
                 T v[RPT];
-#pragma unroll
-                for (int i = 0; i < RPT; ++i) v[i] = S.vbuf[b][lane + 32 * i];
+                VbufLayout<T, RPT>::load(S.vbuf[b], lane, vsw, v);
                 const T tau = S.taub[b];
                 T q[CW];
 #pragma unroll
