@@ -32,7 +32,9 @@ struct TcApplySmem {
     uint32_t b_hi[NMAX * NMAX];    // K-major B operand: W (K = NMAX rows of W, N = NMAX)
     uint32_t b_lo[NMAX * NMAX];
     float Vt[NMAX][NMAX + 1];      // masked top block of V (read again by block 0)
-    float Bs[NMAX][NMAX + 1];      // the parent block B (read again by the epilogue)
+    // the parent block B (read again by the epilogue); rows padded to 16
+    // bytes so the W products read a row's columns as vectors
+    __align__(16) float Bs[NMAX][NMAX + 4];
     union {
         struct {                   // K-major A operand, one 128-row block
             uint32_t a_hi[128 * NMAX];
@@ -40,7 +42,7 @@ struct TcApplySmem {
         } op;
         struct {                   // scratch of the W products, dead before staging starts
             float Tt[NMAX][NMAX + 1];
-            float Ys[NMAX][NMAX + 1];
+            __align__(16) float Ys[NMAX][NMAX + 4];
         } w;
     } u;
     unsigned long long mbar;
@@ -117,22 +119,40 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
             }
         }
         __syncthreads();
-        // Each thread owns output row k and CPT columns c0 + CS*j: CPT
-        // independent accumulators per pass instead of serial dot chains.
-        constexpr int CPT = NMAX * NMAX / 128, CS = 128 / NMAX;
-        const int k = tid % NMAX, c0 = tid / NMAX;
+        // Each thread owns output row k and the CPT contiguous columns
+        // c0 .. c0+CPT-1: per term one shared load of its own operand and
+        // CPT/4 16-byte loads of the other, which every lane of the warp
+        // reads at the same address (broadcast).
+        constexpr int CPT = NMAX * NMAX / 128;
+        static_assert(CPT % 2 == 0 && CPT <= 8, "W products read 8- or 16-byte groups");
+        const int k = tid % NMAX, c0 = (tid / NMAX) * CPT;
+        auto row_terms = [&](const float* row, float(&a)[CPT], float x) {
+            if constexpr (CPT % 4 == 0) {
+#pragma unroll
+                for (int j = 0; j < CPT; j += 4) {
+                    const float4 q = *reinterpret_cast<const float4*>(row + c0 + j);
+                    a[j] = fmaf(x, q.x, a[j]);
+                    a[j + 1] = fmaf(x, q.y, a[j + 1]);
+                    a[j + 2] = fmaf(x, q.z, a[j + 2]);
+                    a[j + 3] = fmaf(x, q.w, a[j + 3]);
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < CPT; j += 2) {
+                    const float2 q = *reinterpret_cast<const float2*>(row + c0 + j);
+                    a[j] = fmaf(x, q.x, a[j]);
+                    a[j + 1] = fmaf(x, q.y, a[j + 1]);
+                }
+            }
+        };
         {
             float acc[CPT];
 #pragma unroll
             for (int j = 0; j < CPT; ++j) acc[j] = 0.f;
 #pragma unroll
-            for (int r = 0; r < NMAX; ++r) {
-                const float vk = S.Vt[r][k];
+            for (int r = 0; r < NMAX; ++r) row_terms(S.Bs[r], acc, S.Vt[r][k]);
 #pragma unroll
-                for (int j = 0; j < CPT; ++j) acc[j] += vk * S.Bs[r][c0 + CS * j];
-            }
-#pragma unroll
-            for (int j = 0; j < CPT; ++j) S.u.w.Ys[k][c0 + CS * j] = acc[j];  // Y = V_top^T B
+            for (int j = 0; j < CPT; ++j) S.u.w.Ys[k][c0 + j] = acc[j];  // Y = V_top^T B
         }
         __syncthreads();
         {
@@ -140,17 +160,13 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
 #pragma unroll
             for (int j = 0; j < CPT; ++j) acc[j] = 0.f;
 #pragma unroll
-            for (int l = 0; l < NMAX; ++l) {
-                const float tkl = S.u.w.Tt[k][l];
-#pragma unroll
-                for (int j = 0; j < CPT; ++j) acc[j] += tkl * S.u.w.Ys[l][c0 + CS * j];
-            }
+            for (int l = 0; l < NMAX; ++l) row_terms(S.u.w.Ys[l], acc, S.u.w.Tt[k][l]);
 #pragma unroll
             for (int j = 0; j < CPT; ++j) {
                 // W = T Y as the B operand (row = output column c, K index k)
                 uint32_t hi, lo;
                 tc::split_tf32(acc[j], hi, lo);
-                const uint32_t off = tc::kmajor_off(c0 + CS * j, k, NMAX) >> 2;
+                const uint32_t off = tc::kmajor_off(c0 + j, k, NMAX) >> 2;
                 S.b_hi[off] = hi;
                 S.b_lo[off] = lo;
             }
