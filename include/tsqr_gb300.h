@@ -148,6 +148,35 @@ tsqr_status tsqr_profile(int kind, int elem_bytes, int64_t m, int64_t n, void* A
                          int64_t ldr, void* work, size_t work_bytes, const tsqr_opts* opts, void* stream,
                          float* launch_ms, int* launch_tag, int max_launch, int* n_launch);
 
+/* Accuracy of a thin QR, computed on the GPU in FP64.  Replaces the
+ * reference's host checker check_QR_accuracy (utils.h:317-455), whose
+ * cuSOLVER gesvd workspace overflows int past m = 46,340.  A is the original
+ * m x n matrix, Q the thin Q (ldq >= m) and R the n x n factor (ldr >= n),
+ * device pointers of element size elem_bytes (4 or 8).  The element gate is
+ * the reference's all_close (utils.h:148-174; the reference passes atol 1e-4,
+ * rtol 1e-5): |(QR)_ij - A_ij| <= max(atol, rtol |A_ij|), NaN fails, and the
+ * first failure is the first in column-major order, as there.  The spectral
+ * figures are the two the reference prints (utils.h:380).  Synchronizes on
+ * `stream`; the result is written to host memory. */
+typedef struct tsqr_check_result {
+    double backward_fro;   /* ||A - QR||_F / ||A||_F                 */
+    double orth_fro;       /* ||Q^T Q - I||_F                        */
+    double backward_2;     /* ||A - QR||_2 / ||A||_2                 */
+    double orth_2;         /* ||I - Q^T Q||_2 / n                    */
+    int64_t gate_failures; /* elements outside the gate              */
+    int64_t first_row;     /* first failing element, -1 if none      */
+    int64_t first_col;
+    double first_value;    /* (QR) at the first failure              */
+    double first_ref;      /* A at the first failure                 */
+} tsqr_check_result;
+
+/* Workspace bytes of tsqr_check: an m x n FP64 residual, the Gram partials
+ * (ceil(m / 4096) x n x n doubles) and three n x n Gram matrices. */
+size_t tsqr_check_workspace_bytes(int64_t m, int64_t n);
+tsqr_status tsqr_check(int elem_bytes, int64_t m, int64_t n, const void* A, int64_t lda, const void* Q, int64_t ldq,
+                       const void* R, int64_t ldr, double atol, double rtol, void* work, size_t work_bytes,
+                       void* stream, tsqr_check_result* out);
+
 /* Human-readable text of a status; never NULL. */
 const char* tsqr_status_string(tsqr_status s);
 

@@ -19,7 +19,7 @@ import os
 
 __all__ = [
     "TsqrError", "PLAIN", "TF32X3", "BF16X3", "lib", "library_path", "tsqr", "qr", "tsqr_", "qr_",
-    "tsqr_batched_", "profile_", "workspace_bytes", "qr_workspace_bytes", "empty_colmajor", "to_colmajor",
+    "tsqr_batched_", "profile_", "check_", "workspace_bytes", "qr_workspace_bytes", "empty_colmajor", "to_colmajor",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -41,6 +41,13 @@ class TsqrError(RuntimeError):
 class Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("reorth", ctypes.c_int), ("panel", ctypes.c_int),
                 ("reserved", ctypes.c_int * 5)]
+
+
+class CheckResult(ctypes.Structure):
+    _fields_ = [("backward_fro", ctypes.c_double), ("orth_fro", ctypes.c_double),
+                ("backward_2", ctypes.c_double), ("orth_2", ctypes.c_double),
+                ("gate_failures", ctypes.c_int64), ("first_row", ctypes.c_int64), ("first_col", ctypes.c_int64),
+                ("first_value", ctypes.c_double), ("first_ref", ctypes.c_double)]
 
 
 _i64 = ctypes.c_int64
@@ -71,6 +78,9 @@ EXPORTS = {
                     ctypes.c_int),
     "tsqr_profile": ([ctypes.c_int, ctypes.c_int, _i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t,
                       ctypes.POINTER(Opts), _p, _p, _p, ctypes.c_int, _p], ctypes.c_int),
+    "tsqr_check_workspace_bytes": ([_i64, _i64], ctypes.c_size_t),
+    "tsqr_check": ([ctypes.c_int, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, ctypes.c_double, ctypes.c_double, _p,
+                    ctypes.c_size_t, _p, ctypes.POINTER(CheckResult)], ctypes.c_int),
     "tsqr_status_string": ([ctypes.c_int], ctypes.c_char_p),
     "tsqr_version": ([], ctypes.c_char_p),
 }
@@ -187,6 +197,28 @@ def _work(nbytes, work, device):
             raise TsqrError(3, "workspace")
         return work, work.numel() * work.element_size()
     return torch.empty(max(nbytes, 1), dtype=torch.uint8, device=device), max(nbytes, 1)
+
+
+def check_(A, Q, R, atol=1e-4, rtol=1e-5, work=None, stream=None):
+    """Accuracy of Q R against the original A (column-major CUDA tensors of
+    one dtype), computed on the GPU in FP64 by tsqr_check.  Returns a dict:
+    backward_fro, orth_fro, backward_2, orth_2 (the reference's two printed
+    figures), gate_failures and the first failing element (row, col, QR
+    value, A value) of the all_close gate with tolerances atol / rtol."""
+    m, n = Q.shape
+    if A.shape != Q.shape or R.shape != (n, n) or A.dtype != Q.dtype or R.dtype != Q.dtype:
+        raise TsqrError(1, "check_: shapes or dtypes disagree")
+    nbytes = int(lib().tsqr_check_workspace_bytes(m, n))
+    w, wb = _work(nbytes, work, Q.device)
+    res = CheckResult()
+    _check(lib().tsqr_check(Q.element_size(), m, n, A.data_ptr(), _ld(A), Q.data_ptr(), _ld(Q), R.data_ptr(), _ld(R),
+                            float(atol), float(rtol), w.data_ptr(), wb, _stream_handle(stream), ctypes.byref(res)),
+           "check_")
+    out = {k: getattr(res, k) for k, _ in CheckResult._fields_}
+    if out["gate_failures"] == 0:
+        out["first_row"] = out["first_col"] = None
+        out["first_value"] = out["first_ref"] = None
+    return out
 
 
 def tsqr_(A, R=None, precision="plain", work=None, stream=None):
