@@ -148,6 +148,33 @@ tsqr_status tsqr_profile(int kind, int elem_bytes, int64_t m, int64_t n, void* A
                          int64_t ldr, void* work, size_t work_bytes, const tsqr_opts* opts, void* stream,
                          float* launch_ms, int* launch_tag, int max_launch, int* n_launch);
 
+/* Implicit-Q form (no counterpart in the reference, which always forms the
+ * explicit thin Q, kernelQR.h:224-290).
+ * tsqr_*_factor runs the up-sweep only.  A keeps level 0 of the compact-WY
+ *   tree (Householder vectors below each tile's diagonal, T in its top
+ *   block), `work` (tsqr_workspace_bytes, PLAIN precision) keeps the upper
+ *   levels, and R is written as by tsqr_*_ex.  Leave A and work unchanged
+ *   while the factorisation is in use.  PLAIN precision only.
+ * tsqr_*_apply_qt: D (n x k, ldd >= n) = Q^T C for C (m x k, ldc >= m),
+ *   walking the same tree upwards; C is only read.  cwork holds the stacked
+ *   intermediate levels: tsqr_apply_qt_workspace_bytes(m, n, k, elem_bytes)
+ *   bytes.  n <= 64 (FP32) / 32 (FP64).
+ * tsqr_*_form_q runs the down-sweep: A becomes the explicit thin Q, exactly
+ *   as tsqr_*_ex leaves it; the tree in A is consumed. */
+tsqr_status tsqr_s_factor(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
+                          size_t work_bytes, const tsqr_opts* opts, void* stream);
+tsqr_status tsqr_d_factor(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr, void* work,
+                          size_t work_bytes, const tsqr_opts* opts, void* stream);
+size_t tsqr_apply_qt_workspace_bytes(int64_t m, int64_t n, int64_t k, int elem_bytes);
+tsqr_status tsqr_s_apply_qt(int64_t m, int64_t n, const float* V, int64_t ldv, const void* work, size_t work_bytes,
+                            int64_t k, const float* C, int64_t ldc, float* D, int64_t ldd, void* cwork,
+                            size_t cwork_bytes, void* stream);
+tsqr_status tsqr_d_apply_qt(int64_t m, int64_t n, const double* V, int64_t ldv, const void* work, size_t work_bytes,
+                            int64_t k, const double* C, int64_t ldc, double* D, int64_t ldd, void* cwork,
+                            size_t cwork_bytes, void* stream);
+tsqr_status tsqr_s_form_q(int64_t m, int64_t n, float* A, int64_t lda, void* work, size_t work_bytes, void* stream);
+tsqr_status tsqr_d_form_q(int64_t m, int64_t n, double* A, int64_t lda, void* work, size_t work_bytes, void* stream);
+
 /* Accuracy of a thin QR, computed on the GPU in FP64.  Replaces the
  * reference's host checker check_QR_accuracy (utils.h:317-455), whose
  * cuSOLVER gesvd workspace overflows int past m = 46,340.  A is the original

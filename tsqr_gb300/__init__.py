@@ -19,7 +19,8 @@ import os
 
 __all__ = [
     "TsqrError", "PLAIN", "TF32X3", "BF16X3", "lib", "library_path", "tsqr", "qr", "tsqr_", "qr_",
-    "tsqr_batched_", "profile_", "check_", "workspace_bytes", "qr_workspace_bytes", "empty_colmajor", "to_colmajor",
+    "tsqr_batched_", "profile_", "check_", "factor_", "apply_qt_", "form_q_", "Factorization", "workspace_bytes",
+    "qr_workspace_bytes", "empty_colmajor", "to_colmajor",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -78,6 +79,15 @@ EXPORTS = {
                     ctypes.c_int),
     "tsqr_profile": ([ctypes.c_int, ctypes.c_int, _i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t,
                       ctypes.POINTER(Opts), _p, _p, _p, ctypes.c_int, _p], ctypes.c_int),
+    "tsqr_s_factor": ([_i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p], ctypes.c_int),
+    "tsqr_d_factor": ([_i64, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p], ctypes.c_int),
+    "tsqr_apply_qt_workspace_bytes": ([_i64, _i64, _i64, ctypes.c_int], ctypes.c_size_t),
+    "tsqr_s_apply_qt": ([_i64, _i64, _p, _i64, _p, ctypes.c_size_t, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t,
+                         _p], ctypes.c_int),
+    "tsqr_d_apply_qt": ([_i64, _i64, _p, _i64, _p, ctypes.c_size_t, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t,
+                         _p], ctypes.c_int),
+    "tsqr_s_form_q": ([_i64, _i64, _p, _i64, _p, ctypes.c_size_t, _p], ctypes.c_int),
+    "tsqr_d_form_q": ([_i64, _i64, _p, _i64, _p, ctypes.c_size_t, _p], ctypes.c_int),
     "tsqr_check_workspace_bytes": ([_i64, _i64], ctypes.c_size_t),
     "tsqr_check": ([ctypes.c_int, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, ctypes.c_double, ctypes.c_double, _p,
                     ctypes.c_size_t, _p, ctypes.POINTER(CheckResult)], ctypes.c_int),
@@ -197,6 +207,68 @@ def _work(nbytes, work, device):
             raise TsqrError(3, "workspace")
         return work, work.numel() * work.element_size()
     return torch.empty(max(nbytes, 1), dtype=torch.uint8, device=device), max(nbytes, 1)
+
+
+class Factorization:
+    """The implicit-Q form left by factor_: A holds level 0 of the
+    compact-WY tree and `work` the upper levels (keep both unchanged while
+    the factorisation is in use); R is the n x n factor."""
+
+    def __init__(self, A, R, work):
+        self.A, self.R, self.work = A, R, work
+
+    @property
+    def shape(self):
+        return tuple(self.A.shape)
+
+
+def factor_(A, R=None, work=None, stream=None):
+    """Up-sweep only (tsqr_*_factor): returns a Factorization; A is
+    overwritten by the tree, not by Q.  Plain precision."""
+    m, n = A.shape
+    lda = _ld(A)
+    if R is None:
+        R = empty_colmajor(n, n, A.dtype, A.device)
+    nbytes = workspace_bytes(m, n, A.dtype)
+    if nbytes == 0:
+        raise TsqrError(2, "factor_")
+    w, wb = _work(nbytes, work, A.device)
+    fn = lib().tsqr_s_factor if A.element_size() == 4 else lib().tsqr_d_factor
+    o = _opts("plain")
+    _check(fn(m, n, A.data_ptr(), lda, R.data_ptr(), _ld(R), w.data_ptr(), wb, ctypes.byref(o),
+              _stream_handle(stream)), "factor_")
+    return Factorization(A, R, w)
+
+
+def apply_qt_(fac, C, D=None, work=None, stream=None):
+    """D = Q^T C (n x k) for C (m x k, column-major) from a Factorization;
+    C is only read."""
+    A = fac.A
+    m, n = A.shape
+    k = C.shape[1]
+    if C.shape[0] != m or C.dtype != A.dtype:
+        raise TsqrError(1, "apply_qt_: C must be m x k of A's dtype")
+    if D is None:
+        D = empty_colmajor(n, k, A.dtype, A.device)
+    nbytes = int(lib().tsqr_apply_qt_workspace_bytes(m, n, k, A.element_size()))
+    if nbytes == 0:
+        raise TsqrError(2, "apply_qt_")
+    cw, cwb = _work(nbytes, work, A.device)
+    fn = lib().tsqr_s_apply_qt if A.element_size() == 4 else lib().tsqr_d_apply_qt
+    wb = fac.work.numel() * fac.work.element_size()
+    _check(fn(m, n, A.data_ptr(), _ld(A), fac.work.data_ptr(), wb, k, C.data_ptr(), _ld(C), D.data_ptr(), _ld(D),
+              cw.data_ptr(), cwb, _stream_handle(stream)), "apply_qt_")
+    return D
+
+
+def form_q_(fac, stream=None):
+    """Down-sweep (tsqr_*_form_q): fac.A becomes the explicit thin Q."""
+    A = fac.A
+    m, n = A.shape
+    fn = lib().tsqr_s_form_q if A.element_size() == 4 else lib().tsqr_d_form_q
+    wb = fac.work.numel() * fac.work.element_size()
+    _check(fn(m, n, A.data_ptr(), _ld(A), fac.work.data_ptr(), wb, _stream_handle(stream)), "form_q_")
+    return A
 
 
 def check_(A, Q, R, atol=1e-4, rtol=1e-5, work=None, stream=None):

@@ -22,7 +22,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-Xptxas", "-warn-spills"]
 
-SOURCES = ["tsqr.cu", "blocked_qr.cu", "abi.cu", "noalloc.cu", "tc_apply.cu", "tc_gemm.cu", "batched.cu", "check.cu"]
+SOURCES = ["tsqr.cu", "blocked_qr.cu", "abi.cu", "noalloc.cu", "tc_apply.cu", "tc_gemm.cu", "batched.cu", "check.cu",
+           "implicit.cu"]
 
 
 def nvcc():

@@ -49,6 +49,25 @@ tsqr_status tsqr_ex(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, 
     return TSQR_ERR_UNSUPPORTED;
 }
 
+// Implicit-Q form: the up-sweep alone, and later the down-sweep alone, on
+// the same tree (plain precision only).
+template <typename T>
+tsqr_status factor_ex(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
+                      const tsqr_opts* op, void* stream) {
+    const tsqr_opts o = opts_or_default(op);
+    tsqr_status st = check_common<T>(m, n, A, lda, R, ldr, o);
+    if (st != TSQR_OK) return st;
+    if (n > max_tsqr_n<T>() || o.precision != TSQR_PRECISION_PLAIN) return TSQR_ERR_UNSUPPORTED;
+    return tsqr::tsqr_plain<T>(m, n, A, lda, R, ldr, work, work_bytes, (cudaStream_t)stream, tsqr::kPhaseUp);
+}
+
+template <typename T>
+tsqr_status form_q_ex(int64_t m, int64_t n, T* A, int64_t lda, void* work, size_t work_bytes, void* stream) {
+    if (m < 1 || n < 1 || m < n || lda < m || A == nullptr) return TSQR_ERR_INVALID_ARG;
+    if (n > max_tsqr_n<T>()) return TSQR_ERR_UNSUPPORTED;
+    return tsqr::tsqr_plain<T>(m, n, A, lda, nullptr, n, work, work_bytes, (cudaStream_t)stream, tsqr::kPhaseDown);
+}
+
 template <typename T>
 tsqr_status qr_ex(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
                   const tsqr_opts* op, void* stream) {
@@ -148,6 +167,21 @@ tsqr_status tsqr_s_ex(int64_t m, int64_t n, float* A, int64_t lda, float* R, int
 tsqr_status tsqr_d_ex(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr, void* work,
                       size_t work_bytes, const tsqr_opts* opts, void* stream) {
     return tsqr_ex<double>(m, n, A, lda, R, ldr, work, work_bytes, opts, stream);
+}
+tsqr_status tsqr_s_factor(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
+                          size_t work_bytes, const tsqr_opts* opts, void* stream) {
+    return factor_ex<float>(m, n, A, lda, R, ldr, work, work_bytes, opts, stream);
+}
+tsqr_status tsqr_d_factor(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr, void* work,
+                          size_t work_bytes, const tsqr_opts* opts, void* stream) {
+    return factor_ex<double>(m, n, A, lda, R, ldr, work, work_bytes, opts, stream);
+}
+tsqr_status tsqr_s_form_q(int64_t m, int64_t n, float* A, int64_t lda, void* work, size_t work_bytes, void* stream) {
+    return form_q_ex<float>(m, n, A, lda, work, work_bytes, stream);
+}
+tsqr_status tsqr_d_form_q(int64_t m, int64_t n, double* A, int64_t lda, void* work, size_t work_bytes,
+                          void* stream) {
+    return form_q_ex<double>(m, n, A, lda, work, work_bytes, stream);
 }
 tsqr_status qr_s_ex(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
                     size_t work_bytes, const tsqr_opts* opts, void* stream) {

@@ -4,6 +4,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "../../include/tsqr_gb300.h"
 
 namespace tsqr {
@@ -26,14 +28,30 @@ inline void log_launch(int tag, cudaStream_t s) {
 }
 // Launch tags: kind * 1000 + level.
 enum { kTagFactor = 1000, kTagApply = 2000, kTagGemmTN = 3000, kTagReduce = 4000, kTagGemmNN = 5000,
-       kTagAxpy = 6000, kTagTc = 7000, kTagBatched = 8000 };
+       kTagAxpy = 6000, kTagTc = 7000, kTagBatched = 8000, kTagApplyQt = 9000 };
 
-// Plain-precision TSQR tree (tsqr.cu).
+// Plain-precision TSQR tree (tsqr.cu).  phases: the up-sweep (factor every
+// level, R out) and / or the down-sweep (explicit Q from the compact-WY
+// tree left in A and the workspace by the up-sweep).
+enum { kPhaseUp = 1, kPhaseDown = 2 };
 template <typename T>
 size_t tsqr_plain_workspace(int64_t m, int64_t n);
 template <typename T>
 tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
-                       cudaStream_t s);
+                       cudaStream_t s, int phases = kPhaseUp | kPhaseDown);
+// One level of the tree as the up-sweep leaves it: h rows (column-major, ld)
+// cut into ntiles tiles of `rows` rows, each holding V below its diagonal
+// and T in its top block's upper triangle; level 0 is A, the last level is
+// the root.
+template <typename T>
+struct TreeLevel {
+    T* M;
+    int64_t ld, h, ntiles;
+    int rows;
+};
+template <typename T>
+tsqr_status tsqr_plain_tree(int64_t m, int64_t n, const T* A, int64_t lda, const void* work, size_t work_bytes,
+                            std::vector<TreeLevel<T>>* out);
 
 // Recursive blocked QR (blocked_qr.cu).
 template <typename T>

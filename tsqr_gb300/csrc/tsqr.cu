@@ -147,7 +147,7 @@ size_t tsqr_plain_workspace(int64_t m, int64_t n) {
 
 template <typename T>
 tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
-                       cudaStream_t s) {
+                       cudaStream_t s, int phases) {
     KernelSet<T> ks = pick((T*)nullptr, (int)n);
     if (!ks.factor) return TSQR_ERR_UNSUPPORTED;
     std::vector<Level<T>> lv;
@@ -155,7 +155,7 @@ tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ld
     if (need > 0 && (work == nullptr || work_bytes < need)) return TSQR_ERR_WORKSPACE;
     const int L = (int)lv.size();
     // up-sweep
-    for (int l = 0; l < L; ++l) {
+    for (int l = 0; l < L && (phases & kPhaseUp); ++l) {
         FactorParams<T> fp;
         fp.M = lv[l].M;
         fp.ld = lv[l].ld;
@@ -173,7 +173,7 @@ tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ld
         log_launch(kTagFactor + l, s);
     }
     // down-sweep
-    for (int l = L - 1; l >= 0; --l) {
+    for (int l = L - 1; l >= 0 && (phases & kPhaseDown); --l) {
         ApplyParams<T> ap;
         ap.M = lv[l].M;
         ap.ld = lv[l].ld;
@@ -350,10 +350,27 @@ tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R
 
 template size_t tsqr_plain_workspace<float>(int64_t, int64_t);
 template size_t tsqr_plain_workspace<double>(int64_t, int64_t);
+template <typename T>
+tsqr_status tsqr_plain_tree(int64_t m, int64_t n, const T* A, int64_t lda, const void* work, size_t work_bytes,
+                            std::vector<TreeLevel<T>>* out) {
+    KernelSet<T> ks = pick((T*)nullptr, (int)n);
+    if (!ks.factor) return TSQR_ERR_UNSUPPORTED;
+    std::vector<Level<T>> lv;
+    size_t need = plan_levels<T>(m, n, const_cast<T*>(A), lda, ks.rows,
+                                 const_cast<char*>(reinterpret_cast<const char*>(work)), &lv);
+    if (need > 0 && (work == nullptr || work_bytes < need)) return TSQR_ERR_WORKSPACE;
+    out->clear();
+    for (const Level<T>& v : lv) out->push_back({v.M, v.ld, v.h, v.ntiles, ks.rows});
+    return TSQR_OK;
+}
+template tsqr_status tsqr_plain_tree<float>(int64_t, int64_t, const float*, int64_t, const void*, size_t,
+                                            std::vector<TreeLevel<float>>*);
+template tsqr_status tsqr_plain_tree<double>(int64_t, int64_t, const double*, int64_t, const void*, size_t,
+                                             std::vector<TreeLevel<double>>*);
 template tsqr_status tsqr_plain<float>(int64_t, int64_t, float*, int64_t, float*, int64_t, void*, size_t,
-                                       cudaStream_t);
+                                       cudaStream_t, int);
 template tsqr_status tsqr_plain<double>(int64_t, int64_t, double*, int64_t, double*, int64_t, void*, size_t,
-                                        cudaStream_t);
+                                        cudaStream_t, int);
 
 // ---------------------------------------------------------------------------
 // TSQR of a matrix in host memory (tsqr_s_host / tsqr_d_host).  The device
