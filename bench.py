@@ -242,6 +242,55 @@ def run_e2e(tg, A0, form, steps, warmup, device):
     return {"ms": ms, "h2d": m * n * 4, "d2h": m * n * 4 + n * n * 4, "backward": back, "orth": orth}
 
 
+def run_implicit(tg, A0, steps, warmup, device, flush):
+    """Least-squares right-hand side Q^T b two ways, plain precision:
+    implicit (factor_ + apply_qt_, the compact-WY tree walked upwards, Q never
+    formed) against explicit (tsqr_, then Q^T b as a cuBLAS product).  Inputs
+    restored and L2 flushed before every step, outside the timed pair."""
+    import torch
+    m, n = A0.shape
+    A = tg.empty_colmajor(m, n, torch.float32, device)
+    R = tg.empty_colmajor(n, n, torch.float32, device)
+    g = torch.Generator(device=device).manual_seed(99)
+    b = torch.randn((m, 1), generator=g, device=device, dtype=torch.float32)
+    work = torch.empty(max(tg.workspace_bytes(m, n, torch.float32), 1), dtype=torch.uint8, device=device)
+    cwork = torch.empty(max(int(tg.lib().tsqr_apply_qt_workspace_bytes(m, n, 1, 4)), 1), dtype=torch.uint8,
+                        device=device)
+    D = tg.empty_colmajor(n, 1, torch.float32, device)
+    stream = torch.cuda.current_stream()
+
+    def implicit():
+        fac = tg.factor_(A, R, work=work, stream=stream)
+        tg.apply_qt_(fac, b, D, work=cwork, stream=stream)
+        return D
+
+    def explicit():
+        tg.tsqr_(A, R, work=work, stream=stream)
+        return A.t() @ b
+
+    out = {}
+    for name, fn in (("implicit", implicit), ("explicit", explicit)):
+        for _ in range(warmup):
+            A.copy_(A0)
+            fn()
+        times = []
+        for _ in range(steps):
+            A.copy_(A0)
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        out[name] = {"ms": sum(times) / len(times), "qtb": res.double().flatten()}
+    d = (out["implicit"]["qtb"] - out["explicit"]["qtb"]).norm() / out["explicit"]["qtb"].norm()
+    return {"what": "Q^T b (k = 1) of the bench matrix, plain FP32",
+            "implicit_ms": out["implicit"]["ms"], "explicit_ms": out["explicit"]["ms"],
+            "implicit_calls": "tsqr_s_factor + tsqr_s_apply_qt", "explicit_calls": "tsqr_s_ex + cuBLAS Q^T b",
+            "rel_diff": d.item()}
+
+
 def cpu_port(m, n, budget_s=20.0, seed=0):
     """The oracle's restatement of the reference TSQR (FP32) on the host."""
     import numpy as np
@@ -533,6 +582,7 @@ def main():
     traffic = TRAFFIC.get((m, n, dom_name))
     roof_t = max(F / (fp32_peak * 1e12), alg_bytes(m, n) / (pk["hbm_gbs"] * 1e9))
     e2e = run_e2e(tg, A0, head, max(3, args.steps // 4), 2, device)
+    implicit = run_implicit(tg, A0, max(3, args.steps // 4), 2, device, flush)
     e2e_val = ws * F / (e2e["ms"] * 1e-3) / 1e12
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -562,6 +612,7 @@ def main():
                 "d2h_bytes_per_step": e2e["d2h"], "ms_per_step": e2e["ms"],
                 "api": "tsqr_s_host (pinned host A in, Q and R out; copies pipelined with the level-0 kernels)",
                 "backward": e2e["backward"], "orth": e2e["orth"]},
+        "implicit_q": implicit,
         "cpu_baseline": cpu, "cpu_lapack": lap,
         "clocks": clocks, "gpu_launches": nl * args.steps, "launches_per_step": nl,
         "forms": {f: ({"ms": v["ms"], "tflops": F / (v["ms"] * 1e-3) / 1e12, "backward": v["backward"],

@@ -153,8 +153,105 @@ __global__ void __launch_bounds__(kNT) apply_qt_tiles(QtParams<T, NMAX> p) {
     }
 }
 
+// Sum of v[0..31] over the warp, scattered: lane l returns the total of
+// index l.  Five halving rounds (16 + 8 + 4 + 2 + 1 shuffles): in the round
+// of offset o a lane keeps the half of its live values selected by bit o of
+// its lane index and adds the partner's copy of that half.
+template <typename T>
+__device__ __forceinline__ T warp_reduce_scatter32(T (&v)[32], int lane) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < o; ++i) {
+            const T send = upper ? v[i] : v[i + o];
+            const T keep = upper ? v[i + o] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0];
+}
+
+// Q^T c for one column c of C (k small): thread rows read V and c directly
+// from global memory (coalesced along each column), Y = V^T c accumulates in
+// registers and is reduced across the CTA (warp reduce-scatter, then the
+// warps' partials through shared memory).  No staging of V, so the kernel
+// streams the level at close to the memory rate.  Tile heights up to 1024.
+template <typename T, int NMAX>
+__global__ void __launch_bounds__(kNT) apply_qt_column(QtParams<T, NMAX> p, int64_t col) {
+    constexpr int NW = kNT / 32;
+    __shared__ T ys[NW][NMAX];
+    __shared__ T yv[NMAX], zv[NMAX];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n = p.n;
+    for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        const int64_t row0 = t * p.rows;
+        const int ht = (int)((p.h - row0) < p.rows ? (p.h - row0) : p.rows);
+        const T* tile = p.M + row0;
+        const T* ct = p.C + row0 + col * p.ldc;
+        T acc[NMAX];
+#pragma unroll
+        for (int j = 0; j < NMAX; ++j) acc[j] = T(0);
+#pragma unroll 1
+        for (int i = 0; i < 4; ++i) {
+            const int r = tid + kNT * i;
+            if (r < ht) {
+                const T cr = ct[r];
+                T v[NMAX];
+#pragma unroll
+                for (int j = 0; j < NMAX; ++j)
+                    v[j] = (j < n && r > j) ? tile[r + (int64_t)j * p.ld] : ((j < n && r == j) ? T(1) : T(0));
+#pragma unroll
+                for (int j = 0; j < NMAX; ++j) acc[j] = fma(v[j], cr, acc[j]);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < NMAX; h += 32) {
+            T part[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) part[j] = acc[h + j];
+            ys[warp][h + lane] = warp_reduce_scatter32(part, lane);
+        }
+        __syncthreads();
+        if (tid < NMAX) {
+            T y = T(0);
+#pragma unroll
+            for (int w = 0; w < NW; ++w) y += ys[w][tid];
+            yv[tid] = y;
+        }
+        __syncthreads();
+        // Z = T^T Y, then the top n rows of c - V Z
+        if (tid < n) {
+            const int j = tid;
+            T z = T(0);
+            for (int i = 0; i <= j; ++i) z = fma((i < ht) ? tile[i + (int64_t)j * p.ld] : T(0), yv[i], z);
+            zv[j] = z;
+        }
+        __syncthreads();
+        if (tid < n) {
+            const int j = tid;
+            T v = ((j < ht) ? ct[j] : T(0)) - zv[j];
+            for (int i = 0; i < j; ++i) v = fma((j < ht) ? -tile[j + (int64_t)i * p.ld] : T(0), zv[i], v);
+            p.out[t * n + j + col * p.ldo] = v;
+        }
+        __syncthreads();  // ys / yv / zv are reused by the next tile
+    }
+}
+
 template <typename T, int NMAX>
 cudaError_t launch_apply_qt(const QtParams<T, NMAX>& p, cudaStream_t s) {
+    if (p.k <= 4 && p.rows <= 4 * kNT) {
+        // a few columns: one streaming pass per column
+        static int sms = 0;
+        if (!sms) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 148;
+        }
+        const int grid = (int)std::min<int64_t>(p.ntiles, (int64_t)sms * 8);
+        for (int64_t c = 0; c < p.k; ++c) apply_qt_column<T, NMAX><<<grid, kNT, 0, s>>>(p, c);
+        return cudaGetLastError();
+    }
     constexpr size_t smem = sizeof(QtSmem<T, NMAX>);
     static const bool attr = cudaFuncSetAttribute(apply_qt_tiles<T, NMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   (int)smem) == cudaSuccess;
