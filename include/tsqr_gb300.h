@@ -47,12 +47,25 @@ typedef enum tsqr_precision {
                                    3-product split, FP32 accumulation in TMEM  */
 } tsqr_precision;
 
+/* Algorithm of qr_*_ex. */
+typedef enum tsqr_qr_algorithm {
+    TSQR_QR_BLOCK_GS = 0,       /* the reference's recursive block Gram-Schmidt
+                                   (block_QR.h:72-95); orthogonality degrades
+                                   with the condition number unless reorth   */
+    TSQR_QR_HOUSEHOLDER = 1     /* blocked Householder: TSQR panels, Householder
+                                   vectors reconstructed from each panel's Q,
+                                   compact-WY trailing updates; orthogonal to
+                                   working precision for any condition number.
+                                   panel <= 32; reorth is ignored            */
+} tsqr_qr_algorithm;
+
 typedef struct tsqr_opts {
     int precision;   /* tsqr_precision; ignored (always PLAIN) for FP64     */
     int reorth;      /* qr only: 1 = second Gram-Schmidt projection (CGS2)  */
     int panel;       /* qr only: panel width at which recursion stops, 0 = 32
                         (the reference's N_B, block_QR.h:5)                 */
-    int reserved[5]; /* must be zero                                        */
+    int algorithm;   /* qr only: tsqr_qr_algorithm, 0 = the reference's     */
+    int reserved[4]; /* must be zero                                        */
 } tsqr_opts;
 
 /* Workspace bytes an ex call needs for an m x n problem of element size

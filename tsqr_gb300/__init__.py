@@ -41,7 +41,7 @@ class TsqrError(RuntimeError):
 
 class Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("reorth", ctypes.c_int), ("panel", ctypes.c_int),
-                ("reserved", ctypes.c_int * 5)]
+                ("algorithm", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 class CheckResult(ctypes.Structure):
@@ -128,11 +128,15 @@ def _check(st, where):
         raise TsqrError(st, where)
 
 
-def _opts(precision="plain", reorth=False, panel=0):
+_ALGO = {"block_gs": 0, "householder": 1, 0: 0, 1: 1}
+
+
+def _opts(precision="plain", reorth=False, panel=0, algorithm="block_gs"):
     o = Opts()
     o.precision = _PREC[precision]
     o.reorth = 1 if reorth else 0
     o.panel = int(panel)
+    o.algorithm = _ALGO[algorithm]
     return o
 
 
@@ -150,8 +154,8 @@ def workspace_bytes(m, n, dtype, precision="plain"):
     return int(lib().tsqr_workspace_bytes(m, n, _elem(dtype), ctypes.byref(o)))
 
 
-def qr_workspace_bytes(m, n, dtype, precision="plain", reorth=False, panel=0):
-    o = _opts(precision, reorth, panel)
+def qr_workspace_bytes(m, n, dtype, precision="plain", reorth=False, panel=0, algorithm="block_gs"):
+    o = _opts(precision, reorth, panel, algorithm)
     return int(lib().qr_workspace_bytes(m, n, _elem(dtype), ctypes.byref(o)))
 
 
@@ -336,15 +340,19 @@ def tsqr_host_(A, Q=None, R=None, precision="plain", work=None, stream=None, dev
     return Q, R
 
 
-def qr_(A, R=None, precision="plain", reorth=False, panel=0, work=None, stream=None):
-    """Recursive blocked QR of the column-major CUDA tensor A in place."""
+def qr_(A, R=None, precision="plain", reorth=False, panel=0, work=None, stream=None, algorithm="block_gs"):
+    """Blocked QR of the column-major CUDA tensor A in place (A <- Q).
+    algorithm "block_gs": the reference's recursive block Gram-Schmidt;
+    "householder": TSQR panels with reconstructed Householder vectors and
+    compact-WY updates (orthogonal to working precision at any condition
+    number)."""
     import torch
     m, n = A.shape
     lda = _ld(A)
     if R is None:
         R = empty_colmajor(n, n, A.dtype, A.device)
     ldr = _ld(R)
-    o = _opts(precision, reorth, panel)
+    o = _opts(precision, reorth, panel, algorithm)
     nbytes = int(lib().qr_workspace_bytes(m, n, A.element_size(), ctypes.byref(o)))
     if nbytes == 0:
         raise TsqrError(2, "qr_ workspace (m=%d n=%d)" % (m, n))

@@ -27,8 +27,9 @@ tsqr_status check_common(int64_t m, int64_t n, const T* A, int64_t lda, const T*
     if (m < 1 || n < 1 || m < n) return TSQR_ERR_INVALID_ARG;
     if (lda < m || ldr < n) return TSQR_ERR_INVALID_ARG;
     if (A == nullptr || R == nullptr) return TSQR_ERR_INVALID_ARG;
-    for (int i = 0; i < 5; ++i)
+    for (int i = 0; i < 4; ++i)
         if (o.reserved[i] != 0) return TSQR_ERR_INVALID_ARG;
+    if (o.algorithm != TSQR_QR_BLOCK_GS && o.algorithm != TSQR_QR_HOUSEHOLDER) return TSQR_ERR_INVALID_ARG;
     if (o.precision < TSQR_PRECISION_PLAIN || o.precision > TSQR_PRECISION_BF16X3) return TSQR_ERR_INVALID_ARG;
     if (o.panel < 0 || o.reorth < 0 || o.reorth > 1) return TSQR_ERR_INVALID_ARG;
     return TSQR_OK;
@@ -217,8 +218,9 @@ tsqr_status tsqr_batched_s(int count, float* const* A, const int64_t* m, const i
     if (count < 0) return TSQR_ERR_INVALID_ARG;
     if (count == 0) return TSQR_OK;
     if (!A || !m || !n || !lda || !R || !ldr) return TSQR_ERR_INVALID_ARG;
-    for (int i = 0; i < 5; ++i)
+    for (int i = 0; i < 4; ++i)
         if (o.reserved[i] != 0) return TSQR_ERR_INVALID_ARG;
+    if (o.algorithm != TSQR_QR_BLOCK_GS && o.algorithm != TSQR_QR_HOUSEHOLDER) return TSQR_ERR_INVALID_ARG;
     if (o.precision != TSQR_PRECISION_PLAIN) return TSQR_ERR_UNSUPPORTED;
     for (int i = 0; i < count; ++i) {
         if (m[i] < 1 || n[i] < 1 || m[i] < n[i] || lda[i] < m[i] || ldr[i] < n[i]) return TSQR_ERR_INVALID_ARG;

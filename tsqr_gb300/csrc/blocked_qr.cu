@@ -334,10 +334,274 @@ tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, c
     return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------------------
+// Blocked Householder QR (tsqr_opts.algorithm = TSQR_QR_HOUSEHOLDER): each
+// b-column panel is factored by TSQR, its Householder vectors are
+// reconstructed from the explicit panel Q (Ballard, Demmel, Grigori,
+// Jacquelin, Knight, Nguyen, "Reconstructing Householder vectors from
+// tall-skinny QR", 2015): Q_p - [S; 0] = Y U by an LU without pivoting whose
+// signs S = -sign(diagonal) keep every pivot at least 1 in magnitude, and
+// T = -U S Y_1^-T gives H_p = I - Y T Y^T with H_p[:, :b] = Q_p S.  The
+// trailing columns get H_p^T A2 = A2 - Y (T^T (Y^T A2)) (two GEMMs), and Q is
+// accumulated backwards, Q = H_1 ... H_P [I; 0], as LAPACK's orgqr does.
+// Orthogonality is then independent of the condition number, unlike the
+// block Gram-Schmidt recursion of the reference (block_QR.h:72-95).
+// ---------------------------------------------------------------------------
+constexpr int kHrMax = 32;  // panel width limit of the Householder path
+
+// Reconstruction of one panel, one CTA.  In: the top bw x bw block of the
+// panel's explicit Q (at Ap, lda) and its TSQR factor Rp (bw x bw, ldrp).
+// Out: the top block rewritten as the unit lower triangular Y_1, U^-1 and T
+// (bw x bw, ld b), and R_h = S Rp into Rout (upper triangle, ldr).
+template <typename T>
+__global__ void __launch_bounds__(256) hr_reconstruct(int bw, T* Ap, int64_t lda, const T* Rp, int ldrp, T* Uinv,
+                                                      T* Tp, int b, T* Rout, int64_t ldr) {
+    __shared__ T W[kHrMax][kHrMax + 1];   // LU in place: U on and above, L below the diagonal
+    __shared__ T Ui[kHrMax][kHrMax + 1];  // U^-1
+    __shared__ T Li[kHrMax][kHrMax + 1];  // Y_1^-1 (unit lower)
+    __shared__ T sgn[kHrMax];
+    const int tid = threadIdx.x;
+    for (int e = tid; e < bw * bw; e += blockDim.x) {
+        const int i = e % bw, j = e / bw;
+        W[i][j] = Ap[i + (int64_t)j * lda];
+    }
+    __syncthreads();
+    for (int i = 0; i < bw; ++i) {
+        if (tid == 0) {
+            const T s = (W[i][i] >= T(0)) ? T(-1) : T(1);
+            sgn[i] = s;
+            W[i][i] -= s;
+        }
+        __syncthreads();
+        for (int r = i + 1 + tid; r < bw; r += blockDim.x) {
+            const T l = W[r][i] / W[i][i];
+            W[r][i] = l;
+            for (int c = i + 1; c < bw; ++c) W[r][c] -= l * W[i][c];
+        }
+        __syncthreads();
+    }
+    // U^-1 column c by back substitution; Y_1^-1 column c by forward substitution
+    for (int c = tid; c < bw; c += blockDim.x) {
+        for (int i = c; i >= 0; --i) {
+            T x = (i == c) ? T(1) : T(0);
+            for (int k = i + 1; k <= c; ++k) x -= W[i][k] * Ui[k][c];
+            Ui[i][c] = x / W[i][i];
+        }
+        for (int i = 0; i < bw; ++i) {
+            T z = (i == c) ? T(1) : T(0);
+            for (int k = c; k < i; ++k) z -= W[i][k] * Li[k][c];
+            Li[i][c] = (i < c) ? T(0) : z;
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < b * b; e += blockDim.x) {
+        const int i = e % b, j = e / b;
+        T t = T(0), u = T(0);
+        if (i < bw && j < bw) {
+            // T = -U S Y_1^-T: sum over i <= k <= j of U(i,k) s_k Y_1^-1(j,k)
+            for (int k = i; k <= j; ++k) t -= W[i][k] * sgn[k] * Li[j][k];
+            u = (i <= j) ? Ui[i][j] : T(0);
+        }
+        Tp[i + (int64_t)j * b] = t;
+        Uinv[i + (int64_t)j * b] = u;
+    }
+    for (int e = tid; e < bw * bw; e += blockDim.x) {
+        const int i = e % bw, j = e / bw;
+        Ap[i + (int64_t)j * lda] = (i > j) ? W[i][j] : ((i == j) ? T(1) : T(0));
+        if (i <= j) Rout[i + (int64_t)j * ldr] = sgn[i] * Rp[i + j * ldrp];
+    }
+}
+
+// Rows of the panel below its top block: y_r = q_r U^-1 (U^-1 upper
+// triangular), in place, one thread per row.
+template <typename T>
+__global__ void __launch_bounds__(256) rows_times_uinv(int64_t rows, int bw, T* Y, int64_t lda, const T* Uinv, int b) {
+    __shared__ T U[kHrMax][kHrMax];
+    for (int e = threadIdx.x; e < b * b; e += blockDim.x) U[e % b][e / b] = Uinv[e];
+    __syncthreads();
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+        T q[kHrMax];
+        for (int k = 0; k < bw; ++k) q[k] = Y[r + (int64_t)k * lda];
+        for (int c = 0; c < bw; ++c) {
+            T y = T(0);
+            for (int k = 0; k <= c; ++k) y = fma(q[k], U[k][c], y);
+            Y[r + (int64_t)c * lda] = y;
+        }
+    }
+}
+
+// X (bw x n2, ld b) = op(T) W for the upper triangular T (ld b): op = T^T when
+// trans (the factor's H^T), T otherwise (the Q accumulation's H).
+template <typename T>
+__global__ void tri_times(int bw, int64_t n2, const T* Tp, int b, bool trans, const T* W, T* X) {
+    const int64_t total = (int64_t)bw * n2;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % bw);
+        const int64_t c = e / bw;
+        T x = T(0);
+        if (trans)
+            for (int k = 0; k <= i; ++k) x = fma(Tp[k + (int64_t)i * b], W[k + c * b], x);
+        else
+            for (int k = i; k < bw; ++k) x = fma(Tp[i + (int64_t)k * b], W[k + c * b], x);
+        X[i + c * b] = x;
+    }
+}
+
+// M = T Y_1^T (bw x bw, ld b) for the panel's columns of Q, one CTA: T upper
+// and Y_1 unit lower, so M(i, c) = sum over i <= k <= c of T(i,k) Y_1(c,k).
+template <typename T>
+__global__ void panel_m(int bw, const T* Y, int64_t lda, const T* Tp, int b, T* M) {
+    for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+        const int i = e % b, c = e / b;
+        T x = T(0);
+        if (i < bw && c < bw)
+            for (int k = i; k <= c; ++k) x = fma(Tp[i + (int64_t)k * b], Y[c + (int64_t)k * lda], x);
+        M[i + (int64_t)c * b] = x;
+    }
+}
+
+// The panel's columns of Q: row r of [I; 0] - Y M, in place over Y, one
+// thread per row (each row reads only itself).
+template <typename T>
+__global__ void __launch_bounds__(256) panel_q_rows(int64_t rows, int bw, T* Y, int64_t lda, const T* M, int b) {
+    __shared__ T Ms[kHrMax][kHrMax + 1];
+    for (int e = threadIdx.x; e < bw * bw; e += blockDim.x) Ms[e % bw][e / bw] = M[(e % bw) + (int64_t)(e / bw) * b];
+    __syncthreads();
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+        T y[kHrMax];
+        for (int k = 0; k < bw; ++k) y[k] = Y[r + (int64_t)k * lda];
+        for (int c = 0; c < bw; ++c) {
+            T q = (r == c) ? T(1) : T(0);
+            for (int k = 0; k < bw; ++k) q = fma(-y[k], Ms[k][c], q);
+            Y[r + (int64_t)c * lda] = q;
+        }
+    }
+}
+
+// Workspace of the Householder path: [status word | panel TSQR | split-K
+// partials | Rp, U^-1, M | W, X | T of every panel], 256-byte aligned parts.
+struct HqrWs {
+    size_t err = 256, tsqr = 0, part = 0, small = 0, wx = 0, tall = 0;
+    size_t total() const { return err + tsqr + part + small + wx + tall; }
+};
+
+template <typename T>
+HqrWs hqr_ws(int64_t m, int64_t n, int b, bool tc) {
+    HqrWs w;
+    const size_t bb = (size_t)round_up((int64_t)(b * b * sizeof(T)), 256);
+    const int64_t P = ceil_div(n, b);
+    for (int64_t p = 0; p < P; ++p) {
+        const int64_t j = p * b, bw = std::min<int64_t>(b, n - j), mp = m - j, n2 = n - j - bw;
+        const size_t tb = tc ? tsqr_precision_workspace(mp, bw) : tsqr_plain_workspace<T>(mp, bw);
+        w.tsqr = std::max(w.tsqr, (size_t)round_up((int64_t)tb, 256));
+        if (n2 > 0) {
+            const GemmPlan gp = tn_plan(bw, n2, mp);
+            w.part = std::max(w.part, (size_t)round_up(gp.nz * bw * n2 * (int64_t)sizeof(T), 256));
+            w.wx = std::max(w.wx, 2 * (size_t)round_up(b * n2 * (int64_t)sizeof(T), 256));
+        }
+    }
+    w.small = 3 * bb;
+    w.tall = (size_t)P * bb;
+    return w;
+}
+
+template <typename T>
+tsqr_status hqr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
+                    const tsqr_opts& o, cudaStream_t s) {
+    const int b = panel_of(o);
+    if (b > kHrMax) return TSQR_ERR_UNSUPPORTED;
+    const bool tc = use_tc<T>(o);
+    const HqrWs w = hqr_ws<T>(m, n, b, tc);
+    if (work == nullptr || work_bytes < w.total()) return TSQR_ERR_WORKSPACE;
+    char* base = static_cast<char*>(work);
+    int* err = reinterpret_cast<int*>(base);
+    char* tws = base + w.err;
+    T* part = reinterpret_cast<T*>(tws + w.tsqr);
+    const size_t bb = (size_t)round_up((int64_t)(b * b * sizeof(T)), 256);
+    char* sm = tws + w.tsqr + w.part;
+    T* Rp = reinterpret_cast<T*>(sm);
+    T* Uinv = reinterpret_cast<T*>(sm + bb);
+    T* Mb = reinterpret_cast<T*>(sm + 2 * bb);
+    T* W = reinterpret_cast<T*>(sm + w.small);
+    T* X = reinterpret_cast<T*>(sm + w.small + w.wx / 2);
+    char* tall = sm + w.small + w.wx;
+    auto Tp = [&](int64_t p) { return reinterpret_cast<T*>(tall + p * bb); };
+    if (tc && cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
+    if (cudaMemset2DAsync(R, ldr * sizeof(T), 0, n * sizeof(T), n, s) != cudaSuccess) return TSQR_ERR_CUDA;
+    const int64_t P = ceil_div(n, b);
+    auto grid_rows = [](int64_t rows) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(rows, 256), 4096)); };
+    // Y X subtracted from A2 (mp x n2), K = bw
+    auto update = [&](int64_t mp, int64_t bw, int64_t n2, const T* Y, T* A2) {
+        if (tc) {
+            update_nn_tc<T>(mp, bw, n2, Y, lda, X, b, A2, err, s);
+        } else {
+            dim3 g((unsigned)ceil_div(mp, kTile), (unsigned)ceil_div(n2, kTile));
+            gemm_nn<T><<<g, 256, 0, s>>>(mp, (int)n2, (int)bw, T(-1), Y, lda, X, b, T(1), A2, lda);
+            log_launch(kTagGemmNN, s);
+        }
+    };
+    auto small_grid = [](int64_t total) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, 256), 1024)); };
+
+    // ---- factor: panel TSQR, reconstruction, trailing update ---------------
+    for (int64_t p = 0; p < P; ++p) {
+        const int64_t j = p * b, bw = std::min<int64_t>(b, n - j), mp = m - j, n2 = n - j - bw;
+        T* Ap = A + j + j * lda;
+        tsqr_status st;
+        if constexpr (std::is_same<T, float>::value) {
+            st = tc ? tsqr_precision(mp, bw, Ap, lda, Rp, bw, tws, w.tsqr, s)
+                    : tsqr_plain<T>(mp, bw, Ap, lda, Rp, bw, tws, w.tsqr, s);
+        } else {
+            st = tsqr_plain<T>(mp, bw, Ap, lda, Rp, bw, tws, w.tsqr, s);
+        }
+        if (st != TSQR_OK) return st;
+        hr_reconstruct<T><<<1, 256, 0, s>>>((int)bw, Ap, lda, Rp, (int)bw, Uinv, Tp(p), b, R + j + j * ldr, ldr);
+        log_launch(kTagHouse, s);
+        if (mp > bw) {
+            rows_times_uinv<T><<<grid_rows(mp - bw), 256, 0, s>>>(mp - bw, (int)bw, Ap + bw, lda, Uinv, b);
+            log_launch(kTagHouse + 1, s);
+        }
+        if (n2 > 0) {
+            T* A2 = A + j + (j + bw) * lda;
+            proj_tn<T>(mp, bw, n2, Ap, A2, lda, part, W, b, T(0), s);                   // W = Y^T A2
+            tri_times<T><<<small_grid(bw * n2), 256, 0, s>>>((int)bw, n2, Tp(p), b, true, W, X);  // X = T^T W
+            log_launch(kTagHouse + 2, s);
+            update(mp, bw, n2, Ap, A2);                                                  // A2 -= Y X
+            if (cudaMemcpy2DAsync(R + j + (j + bw) * ldr, ldr * sizeof(T), A2, lda * sizeof(T), bw * sizeof(T), n2,
+                                  cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+                return TSQR_ERR_CUDA;
+        }
+    }
+
+    // ---- Q = H_1 ... H_P [I; 0], accumulated backwards in A ---------------
+    for (int64_t p = 1; p < P; ++p) {
+        // rows above panel p's diagonal block (R entries) become Q's zeros
+        const int64_t j = p * b, bw = std::min<int64_t>(b, n - j);
+        if (cudaMemset2DAsync(A + j * lda, lda * sizeof(T), 0, j * sizeof(T), bw, s) != cudaSuccess)
+            return TSQR_ERR_CUDA;
+    }
+    for (int64_t p = P - 1; p >= 0; --p) {
+        const int64_t j = p * b, bw = std::min<int64_t>(b, n - j), mp = m - j, n2 = n - j - bw;
+        T* Ap = A + j + j * lda;
+        if (n2 > 0) {
+            T* A2 = A + j + (j + bw) * lda;
+            proj_tn<T>(mp, bw, n2, Ap, A2, lda, part, W, b, T(0), s);                   // W = Y^T Q_sub
+            tri_times<T><<<small_grid(bw * n2), 256, 0, s>>>((int)bw, n2, Tp(p), b, false, W, X);  // X = T W
+            log_launch(kTagHouse + 2, s);
+            update(mp, bw, n2, Ap, A2);                                                  // Q_sub -= Y X
+        }
+        panel_m<T><<<1, 256, 0, s>>>((int)bw, Ap, lda, Tp(p), b, Mb);
+        panel_q_rows<T><<<grid_rows(mp), 256, 0, s>>>(mp, (int)bw, Ap, lda, Mb, b);
+        log_launch(kTagHouse + 3, s);
+    }
+    return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
+}
+
 }  // namespace
 
 template <typename T>
 size_t qr_workspace(int64_t m, int64_t n, const tsqr_opts& o) {
+    if (o.algorithm == TSQR_QR_HOUSEHOLDER)
+        return panel_of(o) <= kHrMax ? hqr_ws<T>(m, n, panel_of(o), use_tc<T>(o)).total() : 0;
     QrWs w;
     qr_ws_walk<T>(m, n, panel_of(o), o.reorth != 0, use_tc<T>(o), &w);
     return w.total();
@@ -346,6 +610,7 @@ size_t qr_workspace(int64_t m, int64_t n, const tsqr_opts& o) {
 template <typename T>
 tsqr_status qr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
                    const tsqr_opts& o, cudaStream_t s) {
+    if (o.algorithm == TSQR_QR_HOUSEHOLDER) return hqr_run<T>(m, n, A, lda, R, ldr, work, work_bytes, o, s);
     QrWs w;
     qr_ws_walk<T>(m, n, panel_of(o), o.reorth != 0, use_tc<T>(o), &w);
     if (work == nullptr || work_bytes < w.total()) return TSQR_ERR_WORKSPACE;

@@ -28,7 +28,7 @@ inline void log_launch(int tag, cudaStream_t s) {
 }
 // Launch tags: kind * 1000 + level.
 enum { kTagFactor = 1000, kTagApply = 2000, kTagGemmTN = 3000, kTagReduce = 4000, kTagGemmNN = 5000,
-       kTagAxpy = 6000, kTagTc = 7000, kTagBatched = 8000, kTagApplyQt = 9000 };
+       kTagAxpy = 6000, kTagTc = 7000, kTagBatched = 8000, kTagApplyQt = 9000, kTagHouse = 10000 };
 
 // Plain-precision TSQR tree (tsqr.cu).  phases: the up-sweep (factor every
 // level, R out) and / or the down-sweep (explicit Q from the compact-WY
