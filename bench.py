@@ -2,7 +2,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--m M] [--n N] [--form auto|plain|tf32x3|bf16x3]
-                    [--workload tsqr|batch|qr] [--dtype f32|f64] [--reorth]
+                    [--workload tsqr|batch|qr] [--dtype f32|f64] [--reorth] [--algorithm block_gs|householder]
 
 One step = one TSQR (A <- Q, R) of the whole matrix through libtsqr_gb300's C
 ABI.  Input: A = U diag(sigma) V^T with U, V orthonormal (QR of seeded
@@ -392,7 +392,7 @@ def run_batch(tg, steps, warmup, device, seed=2024):
     return out
 
 
-def run_qr(tg, m, n, dtype, forms, reorth, steps, warmup, device, kappa=1e4, seed=77):
+def run_qr(tg, m, n, dtype, forms, reorth, steps, warmup, device, kappa=1e4, seed=77, algorithm="block_gs"):
     """Recursive blocked QR (qr_, the reference's qr<T>) of A = U diag(sigma)
     V^T with sigma geometric 1 -> 1/kappa: every form timed with CUDA events
     on its stream (A restored and L2 flushed before each step, outside the
@@ -409,7 +409,7 @@ def run_qr(tg, m, n, dtype, forms, reorth, steps, warmup, device, kappa=1e4, see
     for f in forms:
         A = A0.t().clone().t()
         R = tg.empty_colmajor(n, n, dtype, device)
-        nb = tg.qr_workspace_bytes(m, n, dtype, precision=f, reorth=reorth)
+        nb = tg.qr_workspace_bytes(m, n, dtype, precision=f, reorth=reorth, algorithm=algorithm)
         if nb == 0:
             out[f] = {"unavailable": "form not offered for this dtype/shape"}
             continue
@@ -422,7 +422,7 @@ def run_qr(tg, m, n, dtype, forms, reorth, steps, warmup, device, kappa=1e4, see
                 flush.zero_()
                 a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 a.record(stream)
-                tg.qr_(A, R, precision=f, reorth=reorth, work=work, stream=stream)
+                tg.qr_(A, R, precision=f, reorth=reorth, work=work, stream=stream, algorithm=algorithm)
                 b.record(stream)
             stream.synchronize()
             if k >= warmup:
@@ -454,6 +454,8 @@ def main():
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"], help="qr workload only")
     ap.add_argument("--reorth", action="store_true", help="qr workload: one reorthogonalisation pass")
     ap.add_argument("--kappa", type=float, default=1e4, help="qr workload: condition number of A")
+    ap.add_argument("--algorithm", default="block_gs", choices=["block_gs", "householder"],
+                    help="qr workload: the reference's block Gram-Schmidt or blocked Householder")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
@@ -523,7 +525,8 @@ def main():
         forms = (["plain", "tf32x3"] if args.dtype == "f32" else ["plain"]) if args.form == "auto" else [args.form]
         sampler = ClockSampler(local)
         sampler.start()
-        res = run_qr(tg, m, n, dt, forms, args.reorth, args.steps, args.warmup, device, kappa=args.kappa)
+        res = run_qr(tg, m, n, dt, forms, args.reorth, args.steps, args.warmup, device, kappa=args.kappa,
+                     algorithm=args.algorithm)
         clocks = sampler.stop()
         bar = 1e-5 if args.dtype == "f32" else 1e-12
         ok = {f: r for f, r in res.items() if "ms" in r and r["backward"] <= bar}
@@ -533,7 +536,8 @@ def main():
                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r.get("ms"),
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
                "data": "synthetic: A = U diag(sigma) V^T, sigma geometric 1..1/%g, seeded" % args.kappa,
-               "config": {"workload": "recursive blocked QR (qr<T>) m=%d n=%d reorth=%s" % (m, n, args.reorth),
+               "config": {"workload": "blocked QR (qr<T>) m=%d n=%d algorithm=%s reorth=%s"
+                                      % (m, n, args.algorithm, args.reorth),
                           "form": head, "l2": "flushed (256 MiB write) before every step"},
                "forms": res, "clocks": clocks}
         if rank == 0:

@@ -363,13 +363,15 @@ def qr_(A, R=None, precision="plain", reorth=False, panel=0, work=None, stream=N
     return R
 
 
-def profile_(kind, A, R, precision="plain", reorth=False, panel=0, work=None, stream=None, max_launch=512):
+def profile_(kind, A, R, precision="plain", reorth=False, panel=0, work=None, stream=None, max_launch=512,
+             algorithm="block_gs"):
     """Run tsqr_ (kind "tsqr") or qr_ (kind "qr") with per-launch device
     timing.  Returns [(tag, ms), ...] in launch order; tag = kind*1000+level
     (1 factor, 2 apply, 3 gemm_tn, 4 reduce, 5 gemm_nn, 6 axpy, 7 tcgen05,
-    8 batched)."""
+    8 batched, 9 apply_qt, 10 Householder reconstruction / small products /
+    panel Q rows)."""
     m, n = A.shape
-    o = _opts(precision, reorth, panel)
+    o = _opts(precision, reorth, panel, algorithm)
     k = 0 if kind == "tsqr" else 1
     nbytes = (lib().tsqr_workspace_bytes if k == 0 else lib().qr_workspace_bytes)(m, n, A.element_size(),
                                                                                  ctypes.byref(o))

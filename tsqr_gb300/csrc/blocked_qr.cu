@@ -351,11 +351,12 @@ constexpr int kHrMax = 32;  // panel width limit of the Householder path
 
 // Reconstruction of one panel, one CTA.  In: the top bw x bw block of the
 // panel's explicit Q (at Ap, lda) and its TSQR factor Rp (bw x bw, ldrp).
-// Out: the top block rewritten as the unit lower triangular Y_1, U^-1 and T
-// (bw x bw, ld b), and R_h = S Rp into Rout (upper triangle, ldr).
+// Out: the top block rewritten as the unit lower triangular Y_1, U^-1
+// (ld kHrMax), T (bw x bw at Tp, ld ldt) and R_h = S Rp into Rout (upper
+// triangle, ldr).
 template <typename T>
 __global__ void __launch_bounds__(256) hr_reconstruct(int bw, T* Ap, int64_t lda, const T* Rp, int ldrp, T* Uinv,
-                                                      T* Tp, int b, T* Rout, int64_t ldr) {
+                                                      T* Tp, int64_t ldt, T* Rout, int64_t ldr) {
     __shared__ T W[kHrMax][kHrMax + 1];   // LU in place: U on and above, L below the diagonal
     __shared__ T Ui[kHrMax][kHrMax + 1];  // U^-1
     __shared__ T Li[kHrMax][kHrMax + 1];  // Y_1^-1 (unit lower)
@@ -394,16 +395,13 @@ __global__ void __launch_bounds__(256) hr_reconstruct(int bw, T* Ap, int64_t lda
         }
     }
     __syncthreads();
-    for (int e = tid; e < b * b; e += blockDim.x) {
-        const int i = e % b, j = e / b;
-        T t = T(0), u = T(0);
-        if (i < bw && j < bw) {
-            // T = -U S Y_1^-T: sum over i <= k <= j of U(i,k) s_k Y_1^-1(j,k)
-            for (int k = i; k <= j; ++k) t -= W[i][k] * sgn[k] * Li[j][k];
-            u = (i <= j) ? Ui[i][j] : T(0);
-        }
-        Tp[i + (int64_t)j * b] = t;
-        Uinv[i + (int64_t)j * b] = u;
+    for (int e = tid; e < bw * bw; e += blockDim.x) {
+        const int i = e % bw, j = e / bw;
+        // T = -U S Y_1^-T: sum over i <= k <= j of U(i,k) s_k Y_1^-1(j,k)
+        T t = T(0);
+        for (int k = i; k <= j; ++k) t -= W[i][k] * sgn[k] * Li[j][k];
+        Tp[i + (int64_t)j * ldt] = t;
+        Uinv[i + j * kHrMax] = (i <= j) ? Ui[i][j] : T(0);
     }
     for (int e = tid; e < bw * bw; e += blockDim.x) {
         const int i = e % bw, j = e / bw;
@@ -415,94 +413,235 @@ __global__ void __launch_bounds__(256) hr_reconstruct(int bw, T* Ap, int64_t lda
 // Rows of the panel below its top block: y_r = q_r U^-1 (U^-1 upper
 // triangular), in place, one thread per row.
 template <typename T>
-__global__ void __launch_bounds__(256) rows_times_uinv(int64_t rows, int bw, T* Y, int64_t lda, const T* Uinv, int b) {
+__global__ void __launch_bounds__(256) rows_times_uinv(int64_t rows, int bw, T* Y, int64_t lda, const T* Uinv) {
     __shared__ T U[kHrMax][kHrMax];
-    for (int e = threadIdx.x; e < b * b; e += blockDim.x) U[e % b][e / b] = Uinv[e];
+    for (int e = threadIdx.x; e < kHrMax * kHrMax; e += blockDim.x) {
+        const int i = e % kHrMax, j = e / kHrMax;
+        U[i][j] = (i < bw && j < bw) ? Uinv[i + j * kHrMax] : T(0);
+    }
     __syncthreads();
+    // compile-time bounds keep the row in registers; columns past bw are zero
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
         T q[kHrMax];
-        for (int k = 0; k < bw; ++k) q[k] = Y[r + (int64_t)k * lda];
-        for (int c = 0; c < bw; ++c) {
+#pragma unroll
+        for (int k = 0; k < kHrMax; ++k) q[k] = (k < bw) ? Y[r + (int64_t)k * lda] : T(0);
+#pragma unroll
+        for (int c = 0; c < kHrMax; ++c) {
             T y = T(0);
+#pragma unroll
             for (int k = 0; k <= c; ++k) y = fma(q[k], U[k][c], y);
-            Y[r + (int64_t)c * lda] = y;
+            if (c < bw) Y[r + (int64_t)c * lda] = y;
         }
     }
 }
 
-// X (bw x n2, ld b) = op(T) W for the upper triangular T (ld b): op = T^T when
-// trans (the factor's H^T), T otherwise (the Q accumulation's H).
+// Products with an upper triangular U (ld ldu), one thread per output:
+//   kind 0: X = alpha U^T W   (p x q; U is p x p)
+//   kind 1: X = alpha U W     (p x q; U is p x p)
+//   kind 2: X = alpha W U     (p x q; U is q x q)
 template <typename T>
-__global__ void tri_times(int bw, int64_t n2, const T* Tp, int b, bool trans, const T* W, T* X) {
-    const int64_t total = (int64_t)bw * n2;
+__global__ void tri_mul(int kind, int p, int64_t q, const T* U, int64_t ldu, const T* W, int64_t ldw, T alpha, T* X,
+                        int64_t ldx) {
+    const int64_t total = (int64_t)p * q;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(e % bw);
-        const int64_t c = e / bw;
+        const int i = (int)(e % p);
+        const int64_t c = e / p;
         T x = T(0);
-        if (trans)
-            for (int k = 0; k <= i; ++k) x = fma(Tp[k + (int64_t)i * b], W[k + c * b], x);
+        if (kind == 0)
+            for (int k = 0; k <= i; ++k) x = fma(U[k + (int64_t)i * ldu], W[k + c * ldw], x);
+        else if (kind == 1)
+            for (int k = i; k < p; ++k) x = fma(U[i + (int64_t)k * ldu], W[k + c * ldw], x);
         else
-            for (int k = i; k < bw; ++k) x = fma(Tp[i + (int64_t)k * b], W[k + c * b], x);
-        X[i + c * b] = x;
+            for (int64_t k = 0; k <= c; ++k) x = fma(W[i + k * ldw], U[k + c * ldu], x);
+        X[i + c * ldx] = alpha * x;
     }
 }
 
-// M = T Y_1^T (bw x bw, ld b) for the panel's columns of Q, one CTA: T upper
-// and Y_1 unit lower, so M(i, c) = sum over i <= k <= c of T(i,k) Y_1(c,k).
+// M = T Y_1^T (bw x bw, ld kHrMax) for the panel's columns of Q, one CTA: T
+// upper (ld ldt) and Y_1 unit lower, so M(i, c) = sum over i <= k <= c of
+// T(i,k) Y_1(c,k).
 template <typename T>
-__global__ void panel_m(int bw, const T* Y, int64_t lda, const T* Tp, int b, T* M) {
-    for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
-        const int i = e % b, c = e / b;
+__global__ void panel_m(int bw, const T* Y, int64_t lda, const T* Tp, int64_t ldt, T* M) {
+    for (int e = threadIdx.x; e < bw * bw; e += blockDim.x) {
+        const int i = e % bw, c = e / bw;
         T x = T(0);
-        if (i < bw && c < bw)
-            for (int k = i; k <= c; ++k) x = fma(Tp[i + (int64_t)k * b], Y[c + (int64_t)k * lda], x);
-        M[i + (int64_t)c * b] = x;
+        for (int k = i; k <= c; ++k) x = fma(Tp[i + (int64_t)k * ldt], Y[c + (int64_t)k * lda], x);
+        M[i + c * kHrMax] = x;
     }
 }
 
 // The panel's columns of Q: row r of [I; 0] - Y M, in place over Y, one
 // thread per row (each row reads only itself).
 template <typename T>
-__global__ void __launch_bounds__(256) panel_q_rows(int64_t rows, int bw, T* Y, int64_t lda, const T* M, int b) {
+__global__ void __launch_bounds__(256) panel_q_rows(int64_t rows, int bw, T* Y, int64_t lda, const T* M) {
     __shared__ T Ms[kHrMax][kHrMax + 1];
-    for (int e = threadIdx.x; e < bw * bw; e += blockDim.x) Ms[e % bw][e / bw] = M[(e % bw) + (int64_t)(e / bw) * b];
+    for (int e = threadIdx.x; e < kHrMax * kHrMax; e += blockDim.x) {
+        const int i = e % kHrMax, j = e / kHrMax;
+        Ms[i][j] = (i < bw && j < bw) ? M[i + j * kHrMax] : T(0);
+    }
     __syncthreads();
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
         T y[kHrMax];
-        for (int k = 0; k < bw; ++k) y[k] = Y[r + (int64_t)k * lda];
-        for (int c = 0; c < bw; ++c) {
+#pragma unroll
+        for (int k = 0; k < kHrMax; ++k) y[k] = (k < bw) ? Y[r + (int64_t)k * lda] : T(0);
+#pragma unroll
+        for (int c = 0; c < kHrMax; ++c) {
             T q = (r == c) ? T(1) : T(0);
-            for (int k = 0; k < bw; ++k) q = fma(-y[k], Ms[k][c], q);
-            Y[r + (int64_t)c * lda] = q;
+#pragma unroll
+            for (int k = 0; k < kHrMax; ++k) q = fma(-y[k], Ms[k][c], q);
+            if (c < bw) Y[r + (int64_t)c * lda] = q;
         }
     }
 }
 
-// Workspace of the Householder path: [status word | panel TSQR | split-K
-// partials | Rp, U^-1, M | W, X | T of every panel], 256-byte aligned parts.
+// The Householder path is recursive, like the block Gram-Schmidt one: the
+// left half is factored, H_1^T is applied to the right half with one GEMM
+// pair of inner dimension n1, the right half's lower rows are factored, and
+// the two compact-WY factors combine, T = [T1, -T1 (Y1^T Y2) T2; 0, T2].  Q
+// is formed the same way backwards.  Every large product is a GEMM of inner
+// dimension >= the panel width, so the tensor-core form applies to it as to
+// block Gram-Schmidt.  Leaves (n <= panel) are TSQR + reconstruction.
+//
+// Workspace: [status word | leaf TSQR | split-K partials | Rp, U^-1, M of a
+// leaf | W, X (n1 x n2 each) | T of the whole matrix (n x n)].
 struct HqrWs {
-    size_t err = 256, tsqr = 0, part = 0, small = 0, wx = 0, tall = 0;
-    size_t total() const { return err + tsqr + part + small + wx + tall; }
+    size_t err = 256, tsqr = 0, part = 0, small = 0, wx = 0, tfull = 0;
+    size_t total() const { return err + tsqr + part + small + wx + tfull; }
 };
+
+template <typename T>
+void hqr_ws_walk(int64_t m, int64_t n, int b, bool tc, HqrWs* w) {
+    if (n <= b) {
+        const size_t tb = tc ? tsqr_precision_workspace(m, n) : tsqr_plain_workspace<T>(m, n);
+        w->tsqr = std::max(w->tsqr, (size_t)round_up((int64_t)tb, 256));
+        return;
+    }
+    const int64_t n1 = split_of(n, b), n2 = n - n1;
+    for (int64_t K : {m, m - n1}) {
+        const int64_t nz = tc_projection(tc, n1, n2) ? tc_tn_splits(n1, n2, K) : tn_plan(n1, n2, K).nz;
+        w->part = std::max(w->part, (size_t)round_up(nz * n1 * n2 * (int64_t)sizeof(T), 256));
+    }
+    w->wx = std::max(w->wx, 2 * (size_t)round_up(n1 * n2 * (int64_t)sizeof(T), 256));
+    hqr_ws_walk<T>(m, n1, b, tc, w);
+    hqr_ws_walk<T>(m - n1, n2, b, tc, w);
+}
 
 template <typename T>
 HqrWs hqr_ws(int64_t m, int64_t n, int b, bool tc) {
     HqrWs w;
-    const size_t bb = (size_t)round_up((int64_t)(b * b * sizeof(T)), 256);
-    const int64_t P = ceil_div(n, b);
-    for (int64_t p = 0; p < P; ++p) {
-        const int64_t j = p * b, bw = std::min<int64_t>(b, n - j), mp = m - j, n2 = n - j - bw;
-        const size_t tb = tc ? tsqr_precision_workspace(mp, bw) : tsqr_plain_workspace<T>(mp, bw);
-        w.tsqr = std::max(w.tsqr, (size_t)round_up((int64_t)tb, 256));
-        if (n2 > 0) {
-            const GemmPlan gp = tn_plan(bw, n2, mp);
-            w.part = std::max(w.part, (size_t)round_up(gp.nz * bw * n2 * (int64_t)sizeof(T), 256));
-            w.wx = std::max(w.wx, 2 * (size_t)round_up(b * n2 * (int64_t)sizeof(T), 256));
-        }
-    }
-    w.small = 3 * bb;
-    w.tall = (size_t)P * bb;
+    hqr_ws_walk<T>(m, n, b, tc, &w);
+    w.small = 3 * (size_t)round_up((int64_t)(b * b * sizeof(T)), 256);
+    w.tfull = (size_t)round_up(n * n * (int64_t)sizeof(T), 256);
     return w;
+}
+
+template <typename T>
+struct HqrCtx {
+    int64_t lda, ldr, ldt;
+    char* tws;
+    size_t tsqr_bytes;
+    T *part, *Rp, *Uinv, *Mb, *W, *X;
+    int* err;
+    bool tc;
+    int b;
+    cudaStream_t s;
+};
+
+inline unsigned grid_of(int64_t work, int64_t cap) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(work, 256), cap));
+}
+
+// C (n1 x n2, ld n1) = A1^T A2 over m rows (A1, A2 share lda)
+template <typename T>
+void hqr_tn(const HqrCtx<T>& c, int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2, T* C) {
+    if (tc_projection(c.tc, n1, n2))
+        proj_tn_tc<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.err, c.s);
+    else
+        proj_tn<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.s);
+}
+
+// A2 (m x n2) -= Y (m x n1) X (n1 x n2, ld n1)
+template <typename T>
+void hqr_nn(const HqrCtx<T>& c, int64_t m, int64_t n1, int64_t n2, const T* Y, const T* X, T* A2) {
+    if (c.tc) {
+        update_nn_tc<T>(m, n1, n2, Y, c.lda, X, n1, A2, c.err, c.s);
+    } else {
+        dim3 g((unsigned)ceil_div(m, kTile), (unsigned)ceil_div(n2, kTile));
+        gemm_nn<T><<<g, 256, 0, c.s>>>(m, (int)n2, (int)n1, T(-1), Y, c.lda, X, n1, T(1), A2, c.lda);
+        log_launch(kTagGemmNN, c.s);
+    }
+}
+
+// Factor the m x n block A (rows and columns from its own origin): Y below
+// its diagonal, R into Rb, T into Tb (ld ldt).
+template <typename T>
+tsqr_status hqr_factor(const HqrCtx<T>& c, int64_t m, int64_t n, T* A, T* Rb, T* Tb) {
+    if (n <= c.b) {
+        tsqr_status st;
+        if constexpr (std::is_same<T, float>::value) {
+            st = c.tc ? tsqr_precision(m, n, A, c.lda, c.Rp, n, c.tws, c.tsqr_bytes, c.s)
+                      : tsqr_plain<T>(m, n, A, c.lda, c.Rp, n, c.tws, c.tsqr_bytes, c.s);
+        } else {
+            st = tsqr_plain<T>(m, n, A, c.lda, c.Rp, n, c.tws, c.tsqr_bytes, c.s);
+        }
+        if (st != TSQR_OK) return st;
+        hr_reconstruct<T><<<1, 256, 0, c.s>>>((int)n, A, c.lda, c.Rp, (int)n, c.Uinv, Tb, c.ldt, Rb, c.ldr);
+        log_launch(kTagHouse, c.s);
+        if (m > n) {
+            rows_times_uinv<T><<<grid_of(m - n, 4096), 256, 0, c.s>>>(m - n, (int)n, A + n, c.lda, c.Uinv);
+            log_launch(kTagHouse + 1, c.s);
+        }
+        return TSQR_OK;
+    }
+    const int64_t n1 = split_of(n, c.b), n2 = n - n1;
+    T* A2 = A + n1 * c.lda;
+    tsqr_status st = hqr_factor<T>(c, m, n1, A, Rb, Tb);
+    if (st != TSQR_OK) return st;
+    // A2 <- H_1^T A2 = A2 - Y1 (T1^T (Y1^T A2))
+    hqr_tn<T>(c, m, n1, n2, A, A2, c.W);
+    tri_mul<T><<<grid_of(n1 * n2, 1024), 256, 0, c.s>>>(0, (int)n1, n2, Tb, c.ldt, c.W, n1, T(1), c.X, n1);
+    log_launch(kTagHouse + 2, c.s);
+    hqr_nn<T>(c, m, n1, n2, A, c.X, A2);
+    if (cudaMemcpy2DAsync(Rb + n1 * c.ldr, c.ldr * sizeof(T), A2, c.lda * sizeof(T), n1 * sizeof(T), n2,
+                          cudaMemcpyDeviceToDevice, c.s) != cudaSuccess)
+        return TSQR_ERR_CUDA;
+    // R12 now lives in R; zeroing it here leaves Y of this block (leaf Y's
+    // with zeros above their unit diagonals) clean for every later product
+    if (cudaMemset2DAsync(A2, c.lda * sizeof(T), 0, n1 * sizeof(T), n2, c.s) != cudaSuccess) return TSQR_ERR_CUDA;
+    T* Tb2 = Tb + n1 + n1 * c.ldt;
+    st = hqr_factor<T>(c, m - n1, n2, A2 + n1, Rb + n1 + n1 * c.ldr, Tb2);
+    if (st != TSQR_OK) return st;
+    // T12 = -T1 (Y1^T Y2) T2, Y2 living in rows n1.. of the block
+    hqr_tn<T>(c, m - n1, n1, n2, A + n1, A2 + n1, c.W);
+    tri_mul<T><<<grid_of(n1 * n2, 1024), 256, 0, c.s>>>(2, (int)n1, n2, Tb2, c.ldt, c.W, n1, T(1), c.X, n1);
+    tri_mul<T><<<grid_of(n1 * n2, 1024), 256, 0, c.s>>>(1, (int)n1, n2, Tb, c.ldt, c.X, n1, T(-1), Tb + n1 * c.ldt,
+                                                         c.ldt);
+    log_launch(kTagHouse + 2, c.s);
+    return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
+}
+
+// Q of the m x n block from its Y (in A) and T (Tb): Q = H [I; 0], in place.
+template <typename T>
+tsqr_status hqr_form_q(const HqrCtx<T>& c, int64_t m, int64_t n, T* A, const T* Tb) {
+    if (n <= c.b) {
+        panel_m<T><<<1, 256, 0, c.s>>>((int)n, A, c.lda, Tb, c.ldt, c.Mb);
+        panel_q_rows<T><<<grid_of(m, 4096), 256, 0, c.s>>>(m, (int)n, A, c.lda, c.Mb);
+        log_launch(kTagHouse + 3, c.s);
+        return TSQR_OK;
+    }
+    const int64_t n1 = split_of(n, c.b), n2 = n - n1;
+    T* A2 = A + n1 * c.lda;
+    // right half first: Q2 = H_2 [I; 0] in rows n1.., zeros above it
+    tsqr_status st = hqr_form_q<T>(c, m - n1, n2, A2 + n1, Tb + n1 + n1 * c.ldt);
+    if (st != TSQR_OK) return st;
+    if (cudaMemset2DAsync(A2, c.lda * sizeof(T), 0, n1 * sizeof(T), n2, c.s) != cudaSuccess) return TSQR_ERR_CUDA;
+    // then H_1 applied to it: A2 - Y1 (T1 (Y1^T A2))
+    hqr_tn<T>(c, m, n1, n2, A, A2, c.W);
+    tri_mul<T><<<grid_of(n1 * n2, 1024), 256, 0, c.s>>>(1, (int)n1, n2, Tb, c.ldt, c.W, n1, T(1), c.X, n1);
+    log_launch(kTagHouse + 2, c.s);
+    hqr_nn<T>(c, m, n1, n2, A, c.X, A2);
+    // the left half last: its Y1 was needed above
+    return hqr_form_q<T>(c, m, n1, A, Tb);
 }
 
 template <typename T>
@@ -514,86 +653,31 @@ tsqr_status hqr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, 
     const HqrWs w = hqr_ws<T>(m, n, b, tc);
     if (work == nullptr || work_bytes < w.total()) return TSQR_ERR_WORKSPACE;
     char* base = static_cast<char*>(work);
-    int* err = reinterpret_cast<int*>(base);
-    char* tws = base + w.err;
-    T* part = reinterpret_cast<T*>(tws + w.tsqr);
+    HqrCtx<T> c;
+    c.lda = lda;
+    c.ldr = ldr;
+    c.ldt = n;
+    c.err = reinterpret_cast<int*>(base);
+    c.tws = base + w.err;
+    c.tsqr_bytes = w.tsqr;
+    c.part = reinterpret_cast<T*>(c.tws + w.tsqr);
     const size_t bb = (size_t)round_up((int64_t)(b * b * sizeof(T)), 256);
-    char* sm = tws + w.tsqr + w.part;
-    T* Rp = reinterpret_cast<T*>(sm);
-    T* Uinv = reinterpret_cast<T*>(sm + bb);
-    T* Mb = reinterpret_cast<T*>(sm + 2 * bb);
-    T* W = reinterpret_cast<T*>(sm + w.small);
-    T* X = reinterpret_cast<T*>(sm + w.small + w.wx / 2);
-    char* tall = sm + w.small + w.wx;
-    auto Tp = [&](int64_t p) { return reinterpret_cast<T*>(tall + p * bb); };
-    if (tc && cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
+    char* sm = c.tws + w.tsqr + w.part;
+    c.Rp = reinterpret_cast<T*>(sm);
+    c.Uinv = reinterpret_cast<T*>(sm + bb);
+    c.Mb = reinterpret_cast<T*>(sm + 2 * bb);
+    c.W = reinterpret_cast<T*>(sm + w.small);
+    c.X = reinterpret_cast<T*>(sm + w.small + w.wx / 2);
+    T* Tfull = reinterpret_cast<T*>(sm + w.small + w.wx);
+    c.tc = tc;
+    c.b = b;
+    c.s = s;
+    if (tc && cudaMemsetAsync(c.err, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
     if (cudaMemset2DAsync(R, ldr * sizeof(T), 0, n * sizeof(T), n, s) != cudaSuccess) return TSQR_ERR_CUDA;
-    const int64_t P = ceil_div(n, b);
-    auto grid_rows = [](int64_t rows) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(rows, 256), 4096)); };
-    // Y X subtracted from A2 (mp x n2), K = bw
-    auto update = [&](int64_t mp, int64_t bw, int64_t n2, const T* Y, T* A2) {
-        if (tc) {
-            update_nn_tc<T>(mp, bw, n2, Y, lda, X, b, A2, err, s);
-        } else {
-            dim3 g((unsigned)ceil_div(mp, kTile), (unsigned)ceil_div(n2, kTile));
-            gemm_nn<T><<<g, 256, 0, s>>>(mp, (int)n2, (int)bw, T(-1), Y, lda, X, b, T(1), A2, lda);
-            log_launch(kTagGemmNN, s);
-        }
-    };
-    auto small_grid = [](int64_t total) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, 256), 1024)); };
-
-    // ---- factor: panel TSQR, reconstruction, trailing update ---------------
-    for (int64_t p = 0; p < P; ++p) {
-        const int64_t j = p * b, bw = std::min<int64_t>(b, n - j), mp = m - j, n2 = n - j - bw;
-        T* Ap = A + j + j * lda;
-        tsqr_status st;
-        if constexpr (std::is_same<T, float>::value) {
-            st = tc ? tsqr_precision(mp, bw, Ap, lda, Rp, bw, tws, w.tsqr, s)
-                    : tsqr_plain<T>(mp, bw, Ap, lda, Rp, bw, tws, w.tsqr, s);
-        } else {
-            st = tsqr_plain<T>(mp, bw, Ap, lda, Rp, bw, tws, w.tsqr, s);
-        }
-        if (st != TSQR_OK) return st;
-        hr_reconstruct<T><<<1, 256, 0, s>>>((int)bw, Ap, lda, Rp, (int)bw, Uinv, Tp(p), b, R + j + j * ldr, ldr);
-        log_launch(kTagHouse, s);
-        if (mp > bw) {
-            rows_times_uinv<T><<<grid_rows(mp - bw), 256, 0, s>>>(mp - bw, (int)bw, Ap + bw, lda, Uinv, b);
-            log_launch(kTagHouse + 1, s);
-        }
-        if (n2 > 0) {
-            T* A2 = A + j + (j + bw) * lda;
-            proj_tn<T>(mp, bw, n2, Ap, A2, lda, part, W, b, T(0), s);                   // W = Y^T A2
-            tri_times<T><<<small_grid(bw * n2), 256, 0, s>>>((int)bw, n2, Tp(p), b, true, W, X);  // X = T^T W
-            log_launch(kTagHouse + 2, s);
-            update(mp, bw, n2, Ap, A2);                                                  // A2 -= Y X
-            if (cudaMemcpy2DAsync(R + j + (j + bw) * ldr, ldr * sizeof(T), A2, lda * sizeof(T), bw * sizeof(T), n2,
-                                  cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-                return TSQR_ERR_CUDA;
-        }
-    }
-
-    // ---- Q = H_1 ... H_P [I; 0], accumulated backwards in A ---------------
-    for (int64_t p = 1; p < P; ++p) {
-        // rows above panel p's diagonal block (R entries) become Q's zeros
-        const int64_t j = p * b, bw = std::min<int64_t>(b, n - j);
-        if (cudaMemset2DAsync(A + j * lda, lda * sizeof(T), 0, j * sizeof(T), bw, s) != cudaSuccess)
-            return TSQR_ERR_CUDA;
-    }
-    for (int64_t p = P - 1; p >= 0; --p) {
-        const int64_t j = p * b, bw = std::min<int64_t>(b, n - j), mp = m - j, n2 = n - j - bw;
-        T* Ap = A + j + j * lda;
-        if (n2 > 0) {
-            T* A2 = A + j + (j + bw) * lda;
-            proj_tn<T>(mp, bw, n2, Ap, A2, lda, part, W, b, T(0), s);                   // W = Y^T Q_sub
-            tri_times<T><<<small_grid(bw * n2), 256, 0, s>>>((int)bw, n2, Tp(p), b, false, W, X);  // X = T W
-            log_launch(kTagHouse + 2, s);
-            update(mp, bw, n2, Ap, A2);                                                  // Q_sub -= Y X
-        }
-        panel_m<T><<<1, 256, 0, s>>>((int)bw, Ap, lda, Tp(p), b, Mb);
-        panel_q_rows<T><<<grid_rows(mp), 256, 0, s>>>(mp, (int)bw, Ap, lda, Mb, b);
-        log_launch(kTagHouse + 3, s);
-    }
-    return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
+    if (cudaMemsetAsync(Tfull, 0, n * n * sizeof(T), s) != cudaSuccess) return TSQR_ERR_CUDA;
+    tsqr_status st = hqr_factor<T>(c, m, n, A, R, Tfull);
+    if (st != TSQR_OK) return st;
+    return hqr_form_q<T>(c, m, n, A, Tfull);
 }
 
 }  // namespace
