@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(32 * (NMAX / CW), MINB) batched_factor_split(c
         const int64_t lt = t - w.tile0;
         const int64_t row0 = lt * B;
         const int ht = (int)((w.h - row0) < B ? (w.h - row0) : B);
-        factor_split_tile<float, NMAX, CW, RPT>(S, w.M + row0, w.ld, ht, w.n, w.Rout + lt * w.n, w.ldr);
+        factor_split_tile<float, NMAX, CW, RPT, false>(S, w.M + row0, w.ld, ht, w.n, w.Rout + lt * w.n, w.ldr);
     }
 }
 

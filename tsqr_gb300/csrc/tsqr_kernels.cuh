@@ -624,12 +624,13 @@ __host__ __device__ constexpr int colsum_stride() {
 // RPT values with KC vector accesses; chunk k of lane l sits at chunk
 // position k ^ ((l / (8 / KC)) & (KC - 1)) of the lane's row, which puts the
 // 8 lanes of each 16-byte access phase on 8 distinct 4-bank groups.
-// Otherwise slot i of lane l is element l + 32 i (scalar accesses).
-template <typename T, int RPT>
+// Otherwise, or when VEC is false, slot i of lane l is element l + 32 i
+// (scalar accesses).
+template <typename T, int RPT, bool VEC = true>
 struct VbufLayout {
     static constexpr int VN = Vec16<T>::N;
     static constexpr int KC = RPT / VN;
-    static constexpr bool kVec = (RPT % VN == 0) && KC >= 1 && KC <= 8 && (KC & (KC - 1)) == 0;
+    static constexpr bool kVec = VEC && (RPT % VN == 0) && KC >= 1 && KC <= 8 && (KC & (KC - 1)) == 0;
     __device__ static int swz(int lane) { return kVec ? (lane / (8 / KC)) & (KC - 1) : 0; }
     template <typename F>
     __device__ static void store(T* buf, int lane, int sw, F&& val) {
@@ -703,7 +704,10 @@ __device__ __forceinline__ T warp_colsum(const T (&q)[CW], T* scratch, int lane)
     return s;
 }
 
-template <typename T, int NMAX, int CW, int RPT>
+// VECV: publish the reflector in the 16-byte vector layout (VbufLayout).
+// Off for the 64-column tile and for the batched kernels, whose registers
+// leave no room for the aligned quads it needs (more spills with it).
+template <typename T, int NMAX, int CW, int RPT, bool VECV = (NMAX <= 32)>
 __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, RPT>& S, T* tile, int64_t ld, int ht,
                                                   int n, T* Rt, int64_t ldr) {
     constexpr int W = NMAX / CW;
@@ -716,10 +720,23 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
     const int col0 = warp * CW;
     const int mycols = max(0, min(CW, n - col0));
     T* scratch = S.xpose[warp];
-    const int vsw = VbufLayout<T, RPT>::swz(lane);
+    using VL = VbufLayout<T, RPT, VECV>;
+    const int vsw = VL::swz(lane);
     // Row lane + 32*i lies strictly below diagonal element j (compile-time
     // true for every slot i >= 1 when NMAX <= 32).
     auto below = [&](int i, int j) { return (NMAX <= 32 && i > 0) || (lane + 32 * i > j); };
+    // Reflector scalars: the branch-free forms shorten the owner's chain for
+    // NMAX <= 32; the 64-column tile, already at its register limit, runs
+    // faster with the plain operations (level-0 factor at 4,194,304 x 64:
+    // 3.25 against 3.78 ms).
+    auto rsq = [](T x) {
+        if constexpr (NMAX <= 32) return refl_sqrt(x);
+        else return sqrt_t(x);
+    };
+    auto rcp = [](T x) {
+        if constexpr (NMAX <= 32) return refl_recip(x);
+        else return recip(x);
+    };
     // x(j, c) of position c, held by lane j % 32 in slot j / 32 (j < 64)
     auto diag_slot = [&](const T(&yy)[RPT][CW], int c, int j) {
         return (NMAX > 32 && j >= 32) ? yy[RPT > 1 ? 1 : 0][c] : yy[0][c];
@@ -766,17 +783,17 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
                 for (int u = 0; u < U; ++u) {
                     const int j = pc0 + base + u;
                     const bool zero = (sig2 == T(0));
-                    const T nrm = refl_sqrt(fmadd(alpha, alpha, sig2));
+                    const T nrm = rsq(fmadd(alpha, alpha, sig2));
                     const T beta = zero ? alpha : ((alpha >= T(0)) ? -nrm : nrm);
-                    const T tau = zero ? T(0) : (beta - alpha) * refl_recip(beta);
-                    const T scale = zero ? T(0) : refl_recip(alpha - beta);
+                    const T tau = zero ? T(0) : (beta - alpha) * rcp(beta);
+                    const T scale = zero ? T(0) : rcp(alpha - beta);
 #pragma unroll
                     for (int i = 0; i < RPT; ++i)
                         if (below(i, j)) y[i][u] *= scale;
                     // v_j of slot i (1 on the diagonal, 0 above it)
                     auto vj = [&](int i) { return below(i, j) ? y[i][u] : ((lane + 32 * i == j) ? T(1) : T(0)); };
                     const int b = j & 1;
-                    VbufLayout<T, RPT>::store(S.vbuf[b], lane, vsw, vj);
+                    VL::store(S.vbuf[b], lane, vsw, vj);
                     if (lane == 0) {
                         S.taub[b] = tau;
                         S.tau[j] = tau;
@@ -845,7 +862,7 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
                 step_barrier(W * 32);
                 const int b = j & 1;
                 T v[RPT];
-                VbufLayout<T, RPT>::load(S.vbuf[b], lane, vsw, v);
+                VL::load(S.vbuf[b], lane, vsw, v);
                 const T tau = S.taub[b];
                 T q[CW];
 #pragma unroll
