@@ -108,3 +108,60 @@ def test_host_entry_argument_checks_need_no_gpu(tg):
     assert call(100, 4, 100, 100, 4, opts=tg._opts("tf32x3"), fn=L.tsqr_d_host) == 2
     assert L.tsqr_host_workspace_bytes(100, 4, 4, ctypes.byref(o)) > 100 * 4 * 4
     assert L.tsqr_host_workspace_bytes(3, 4, 4, ctypes.byref(o)) == 0
+
+
+def test_implicit_q_and_checker_argument_checks_need_no_gpu(tg):
+    """tsqr_*_factor / tsqr_*_apply_qt / tsqr_*_form_q / tsqr_check reject
+    bad sizes, leading dimensions, options and workspaces before any CUDA
+    call, and their workspace queries answer on the CPU."""
+    L = tg.lib()
+    fake = ctypes.c_void_p(0x1000)
+    o = tg._opts("plain")
+    # factor: the tsqr_*_ex checks, plain precision only
+    assert L.tsqr_s_factor(100, 8, fake, 99, fake, 8, fake, 1 << 20, ctypes.byref(o), None) == 1
+    assert L.tsqr_s_factor(3, 8, fake, 3, fake, 8, fake, 1 << 20, ctypes.byref(o), None) == 1
+    assert L.tsqr_s_factor(100, 8, fake, 100, fake, 8, fake, 1 << 20, ctypes.byref(tg._opts("tf32x3")), None) == 2
+    assert L.tsqr_d_factor(100, 33, fake, 100, fake, 33, fake, 1 << 20, ctypes.byref(o), None) == 2
+    assert L.tsqr_s_factor(1 << 20, 32, fake, 1 << 20, fake, 32, fake, 16, ctypes.byref(o), None) == 3
+    # apply_qt
+    args = lambda m, n, ldv, k, ldc, ldd, cwb: (m, n, fake, ldv, fake, 1 << 30, k, fake, ldc, fake, ldd, fake, cwb,
+                                                None)
+    assert L.tsqr_s_apply_qt(*args(100, 8, 99, 3, 100, 8, 1 << 20)) == 1   # ldv < m
+    assert L.tsqr_s_apply_qt(*args(100, 8, 100, 0, 100, 8, 1 << 20)) == 1  # k < 1
+    assert L.tsqr_s_apply_qt(*args(100, 8, 100, 3, 99, 8, 1 << 20)) == 1   # ldc < m
+    assert L.tsqr_s_apply_qt(*args(100, 8, 100, 3, 100, 7, 1 << 20)) == 1  # ldd < n
+    assert L.tsqr_s_apply_qt(*args(100, 65, 100, 3, 100, 65, 1 << 20)) == 2
+    assert L.tsqr_d_apply_qt(*args(100, 33, 100, 3, 100, 33, 1 << 20)) == 2
+    need = L.tsqr_apply_qt_workspace_bytes(1 << 20, 32, 5, 4)
+    assert need > 0 and L.tsqr_apply_qt_workspace_bytes(100, 200, 5, 4) == 0
+    assert L.tsqr_s_apply_qt(*args(1 << 20, 32, 1 << 20, 5, 1 << 20, 32, need - 1)) == 3
+    # form_q
+    assert L.tsqr_s_form_q(100, 8, fake, 99, fake, 1 << 20, None) == 1
+    assert L.tsqr_d_form_q(100, 40, fake, 100, fake, 1 << 20, None) == 2
+    # checker
+    res = tg.CheckResult()
+    chk = lambda eb, m, n, lda, ldq, ldr, wb: L.tsqr_check(eb, m, n, fake, lda, fake, ldq, fake, ldr, 1e-4, 1e-5, fake,
+                                                           wb, None, ctypes.byref(res))
+    assert chk(4, 100, 8, 99, 100, 8, 1 << 20) == 1
+    assert chk(4, 100, 8, 100, 99, 8, 1 << 20) == 1
+    assert chk(4, 100, 8, 100, 100, 7, 1 << 20) == 1
+    assert chk(3, 100, 8, 100, 100, 8, 1 << 20) == 1
+    assert chk(8, 100, 8, 100, 100, 8, 16) == 3
+    assert L.tsqr_check_workspace_bytes(1000, 32) >= 8 * 1000 * 32
+    assert L.tsqr_check_workspace_bytes(0, 32) == 0
+
+
+def test_qr_algorithm_option(tg):
+    """The Householder algorithm of qr_*_ex: workspace query, panel limit,
+    and an unknown algorithm rejected before any CUDA call."""
+    L = tg.lib()
+    fake = ctypes.c_void_p(0x1000)
+    assert tg.qr_workspace_bytes(131072, 512, "float32", algorithm="householder") > 0
+    assert tg.qr_workspace_bytes(131072, 512, "float32", algorithm="householder", panel=64) == 0
+    o = tg._opts("plain")
+    o.algorithm = 5
+    assert L.qr_s_ex(1000, 64, fake, 1000, fake, 64, fake, 1 << 30, ctypes.byref(o), None) == 1
+    o = tg._opts("plain", algorithm="householder", panel=64)
+    assert L.qr_s_ex(1000, 64, fake, 1000, fake, 64, fake, 1 << 30, ctypes.byref(o), None) == 2
+    o = tg._opts("plain", algorithm="householder")
+    assert L.qr_s_ex(1000, 64, fake, 1000, fake, 64, fake, 16, ctypes.byref(o), None) == 3
