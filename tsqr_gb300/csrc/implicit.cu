@@ -93,17 +93,33 @@ __global__ void __launch_bounds__(kNT) apply_qt_tiles(QtParams<T, NMAX> p) {
 #pragma unroll
         for (int s = 0; s < JPT; ++s) acc[s] = T(0);
         for (int r0 = 0; r0 < ht; r0 += kCH) {
-            for (int e = tid; e < kCH * NMAX; e += kNT) {
+            constexpr int PV = kCH * NMAX / kNT, PC = kCH * kKB / kNT;
+            T gv[PV], gc[PC];
+#pragma unroll
+            for (int q = 0; q < PV; ++q) {
+                const int e = tid + kNT * q;
                 const int r = e % kCH, j = e / kCH;
-                const int rr = r0 + r;  // tile row
-                T v = T(0);
-                if (rr < ht && j < n) v = (rr > j) ? tile[rr + (int64_t)j * p.ld] : ((rr == j) ? T(1) : T(0));
-                S.Vs[r][vcol<NMAX>(r, j)] = v;
+                const int rr = r0 + r;
+                gv[q] = (rr < ht && j < n && rr > j) ? tile[rr + (int64_t)j * p.ld] : T(0);
             }
-            for (int e = tid; e < kCH * kKB; e += kNT) {
+#pragma unroll
+            for (int q = 0; q < PC; ++q) {
+                const int e = tid + kNT * q;
                 const int r = e % kCH, cc = e / kCH;
                 const int rr = r0 + r;
-                S.Cs[r][cc] = (rr < ht && c0 + cc < p.k) ? ct[rr + (c0 + cc) * p.ldc] : T(0);
+                gc[q] = (rr < ht && c0 + cc < p.k) ? ct[rr + (c0 + cc) * p.ldc] : T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < PV; ++q) {
+                const int e = tid + kNT * q;
+                const int r = e % kCH, j = e / kCH;
+                const int rr = r0 + r;
+                S.Vs[r][vcol<NMAX>(r, j)] = (rr == j && j < n && rr < ht) ? T(1) : gv[q];
+            }
+#pragma unroll
+            for (int q = 0; q < PC; ++q) {
+                const int e = tid + kNT * q;
+                S.Cs[e % kCH][e / kCH] = gc[q];
             }
             __syncthreads();
             const int rmax = min(kCH, ht - r0);
