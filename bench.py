@@ -162,7 +162,7 @@ def make_input(m, n, seed, device):
 
 
 def check_errors(A0, Q, R):
-    """FP64 backward error and orthogonality on the device (checker)."""
+    """FP64 backward error and orthogonality on the device."""
     import torch
     A64 = A0.double()
     E = A64 - Q.double() @ R.double()

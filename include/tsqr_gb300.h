@@ -189,7 +189,7 @@ tsqr_status tsqr_s_form_q(int64_t m, int64_t n, float* A, int64_t lda, void* wor
 tsqr_status tsqr_d_form_q(int64_t m, int64_t n, double* A, int64_t lda, void* work, size_t work_bytes, void* stream);
 
 /* Accuracy of a thin QR, computed on the GPU in FP64.  Replaces the
- * reference's host checker check_QR_accuracy (utils.h:317-455), whose
+ * reference's host accuracy check check_QR_accuracy (utils.h:317-455), whose
  * cuSOLVER gesvd workspace overflows int past m = 46,340.  A is the original
  * m x n matrix, Q the thin Q (ldq >= m) and R the n x n factor (ldr >= n),
  * device pointers of element size elem_bytes (4 or 8).  The element gate is

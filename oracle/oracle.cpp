@@ -2,7 +2,7 @@
 //
 // TEST INFRASTRUCTURE ONLY.  Nothing in the tsqr_gb300 product links, loads
 // or calls this file; only tests/, the smoke check and the CPU-baseline leg
-// of bench.py use it, as the checker.
+// of bench.py use it, to check results.
 //
 // Contents (each function cites the reference file:line it restates):
 //   * orc_fill_uniform_{f,d}   the reference's seeded input stream
@@ -421,7 +421,7 @@ std::vector<double> gram(int64_t m, int64_t n, F row) {
 // out[2] = ||A - QR||_2 / ||A||_2            (utils.h:353, first figure)
 // out[3] = ||I - Q^T Q||_2 / n               (utils.h:353-354, second figure)
 // All in FP64 regardless of T.  R is read as a full n x n matrix, as the
-// reference's checker does (utils.h:384-385).
+// reference's accuracy check does (utils.h:384-385).
 template <typename T>
 void metrics(int64_t m, int64_t n, const T* A0, int64_t lda0, const T* Q,
              int64_t ldq, const T* R, int64_t ldr, double* out) {

@@ -1,6 +1,6 @@
 """Python binding of the oracle (TEST INFRASTRUCTURE ONLY).
 
-The oracle is the checker: tests/, the smoke check and bench.py's CPU
+The oracle is test infrastructure: tests/, the smoke check and bench.py's CPU
 baseline leg call it; the tsqr_gb300 product never does.  Matrices are numpy
 arrays in Fortran (column-major) order, like the reference's buffers
 (lda = m, test_tsqr.cu:30).
@@ -152,8 +152,8 @@ def metrics(A0, Q, R):
 
     backward:    ||A0 - QR||_F / ||A0||_F
     orth:        ||Q^T Q - I||_F
-    backward_2:  ||A0 - QR||_2 / ||A0||_2      (reference checker, utils.h:353)
-    orth_2_n:    ||I - Q^T Q||_2 / n           (reference checker, utils.h:353)
+    backward_2:  ||A0 - QR||_2 / ||A0||_2      (the reference's printed figure, utils.h:353)
+    orth_2_n:    ||I - Q^T Q||_2 / n           (the reference's printed figure, utils.h:353)
     """
     dt = np.result_type(A0.dtype, Q.dtype, R.dtype)
     if dt not in (np.float32, np.float64):

@@ -110,7 +110,7 @@ def test_host_entry_argument_checks_need_no_gpu(tg):
     assert L.tsqr_host_workspace_bytes(3, 4, 4, ctypes.byref(o)) == 0
 
 
-def test_implicit_q_and_checker_argument_checks_need_no_gpu(tg):
+def test_implicit_q_and_accuracy_check_argument_checks_need_no_gpu(tg):
     """tsqr_*_factor / tsqr_*_apply_qt / tsqr_*_form_q / tsqr_check reject
     bad sizes, leading dimensions, options and workspaces before any CUDA
     call, and their workspace queries answer on the CPU."""
@@ -138,7 +138,7 @@ def test_implicit_q_and_checker_argument_checks_need_no_gpu(tg):
     # form_q
     assert L.tsqr_s_form_q(100, 8, fake, 99, fake, 1 << 20, None) == 1
     assert L.tsqr_d_form_q(100, 40, fake, 100, fake, 1 << 20, None) == 2
-    # checker
+    # accuracy check
     res = tg.CheckResult()
     chk = lambda eb, m, n, lda, ldq, ldr, wb: L.tsqr_check(eb, m, n, fake, lda, fake, ldq, fake, ldr, 1e-4, 1e-5, fake,
                                                            wb, None, ctypes.byref(res))

@@ -1,5 +1,5 @@
-"""GPU tests of the device accuracy checker tsqr_check (check_ in Python),
-which replaces the reference's host checker check_QR_accuracy
+"""GPU tests of the device accuracy check tsqr_check (check_ in Python),
+which replaces the reference's host accuracy check check_QR_accuracy
 (utils.h:317-455).
 
 Bar: its four figures equal the FP64 oracle's (orc.metrics) on the same
@@ -35,7 +35,7 @@ def close(a, b, rtol, atol=1e-300):
 
 @pytest.mark.parametrize("kind,m,n,dtype,precision", [
     ("tsqr", 27648, 32, np.float32, "plain"),
-    ("tsqr", 100000, 32, np.float32, "tf32x3"),  # past the reference checker's m = 46,340 limit
+    ("tsqr", 100000, 32, np.float32, "tf32x3"),  # past the reference check's m = 46,340 limit
     ("tsqr", 1000, 13, np.float64, "plain"),
     ("tsqr", 70001, 64, np.float32, "plain"),
     ("qr", 27648, 128, np.float32, "plain"),
@@ -53,7 +53,7 @@ def test_figures_match_oracle(orc, cuda, tg, kind, m, n, dtype, precision):
     assert res["gate_failures"] == 0 and res["first_row"] is None, res
     # FP64 inputs: the figures (~1e-15) are at the rounding level of forming
     # the Gram matrices in FP64 (about sqrt(m) u64 per entry), so two FP64
-    # checkers agree only to that absolute level
+    # implementations agree only to that absolute level
     atol = 4 * np.sqrt(m) * n * 2.0 ** -53 if dtype == np.float64 else 1e-300
     assert close(res["backward_fro"], met["backward"], 1e-6, atol), (res, met)
     assert close(res["orth_fro"], met["orth"], 1e-6, atol), (res, met)
@@ -103,7 +103,7 @@ def test_gate_counts_nan(orc, cuda, tg):
     assert (res["first_row"], res["first_col"]) == (123, 0)
 
 
-def test_checker_rejects_bad_arguments(cuda, tg):
+def test_check_rejects_bad_arguments(cuda, tg):
     import ctypes
     import torch
     L = tg.lib()

@@ -8,7 +8,7 @@ Tolerances (FP32 u = 2^-24, FP64 u = 2^-53), after normalising diag(R) >= 0:
   (inputs here are well conditioned; kappa-dependent cases check only the
    first two figures).
 At full size (4,194,304 rows) the size-independent figures are computed in
-FP64 on the GPU with torch as the checker.
+FP64 on the GPU with torch.
 """
 import numpy as np
 import pytest
@@ -136,7 +136,7 @@ def test_tsqr_ill_conditioned_is_backward_stable(orc, cuda, tg, kappa):
 
 
 def gpu_metrics(A_dev_orig, Q, R):
-    """FP64 checker on the GPU for full-size problems."""
+    """FP64 error figures on the GPU for full-size problems."""
     import torch
     A64 = A_dev_orig.double()
     Q64 = Q.double()

@@ -12,7 +12,7 @@
 // printed figures (|A-QR|/|A| and |I-Q^TQ|/n in spectral norm; utils.h:353)
 // and the same timing protocol and line (warm-up then repeats, each
 // re-uploading A outside the timed region; "tsqr Latency: x ms";
-// test_tsqr.cu:62-90).  The checker is the library's tsqr_check: the gate and
+// test_tsqr.cu:62-90).  The accuracy check is the library's tsqr_check: the gate and
 // both figures computed on the GPU in FP64 (Gram matrices, largest
 // eigenvalue by Jacobi) instead of cuBLAS + cuSOLVER gesvd on a host copy.
 // A final JSON line adds TFLOP/s and the Frobenius figures.

@@ -1,6 +1,6 @@
 // check.cu -- accuracy of a thin QR on the GPU (tsqr_check).
 //
-// Replaces the reference's host-driven checker check_QR_accuracy
+// Replaces the reference's host-driven accuracy check check_QR_accuracy
 // (utils.h:317-455): there QR = Q R is formed by cuBLAS, copied to the host
 // and compared element by element (all_close, utils.h:148-174, atol 1e-4 /
 // rtol 1e-5), and the two printed figures ||A - QR||_2 / ||A||_2 and
