@@ -118,3 +118,21 @@ def test_check_rejects_bad_arguments(cuda, tg):
     assert call(2, 100, 8, 100, 8, 1 << 20) == 1  # element size
     assert call(4, 100, 8, 100, 8, 64) == 3       # workspace too small
     assert call(4, 100, 8, 100, 8, 1 << 20) == 0
+
+
+def test_check_with_padded_leading_dimensions(orc, cuda, tg):
+    import torch
+    m, n = 20000, 20
+    A0 = orc.fill_uniform(m, n, np.float64, seed=44)
+    dA0 = tg.empty_colmajor(m, n, torch.float64, "cuda", ld=m + 3)
+    dA0.copy_(torch.from_numpy(np.ascontiguousarray(A0)))
+    Q = tg.empty_colmajor(m, n, torch.float64, "cuda", ld=m + 9)
+    Q.copy_(dA0)
+    R = tg.empty_colmajor(n, n, torch.float64, "cuda", ld=n + 4)
+    tg.tsqr_(Q, R)
+    torch.cuda.synchronize()
+    res = tg.check_(dA0, Q, R)
+    met = orc.metrics(A0, to_host(Q), to_host(R))
+    atol = 4 * np.sqrt(m) * n * 2.0 ** -53
+    assert res["gate_failures"] == 0
+    assert close(res["backward_fro"], met["backward"], 1e-6, atol) and close(res["orth_fro"], met["orth"], 1e-6, atol)

@@ -91,3 +91,17 @@ def test_householder_rejects_wide_panels(cuda, tg):
     A = tg.empty_colmajor(1000, 100, torch.float32, "cuda")
     with pytest.raises(tg.TsqrError):
         tg.qr_(A, algorithm="householder", panel=64)
+
+
+def test_householder_with_padded_leading_dimensions(orc, cuda, tg):
+    import torch
+    m, n = 9000, 70
+    A0 = orc.fill_uniform(m, n, np.float32, seed=64)
+    A = tg.empty_colmajor(m, n, torch.float32, "cuda", ld=m + 7)
+    A.copy_(torch.from_numpy(np.ascontiguousarray(A0)))
+    R = tg.empty_colmajor(n, n, torch.float32, "cuda", ld=n + 3)
+    tg.qr_(A, R, algorithm="householder")
+    torch.cuda.synchronize()
+    met = orc.metrics(A0, to_host(A), to_host(R))
+    u = 2.0 ** -24
+    assert met["backward"] <= 10 * n * u and met["orth"] <= 10 * n * u, met

@@ -104,3 +104,27 @@ def test_implicit_rejects_bad_arguments(cuda, tg):
     assert L.tsqr_s_apply_qt(*args(100, 8, 100, 100, 7, 1 << 20)) == 1  # ldd < n
     assert L.tsqr_s_apply_qt(*args(100, 80, 100, 100, 80, 1 << 20)) == 2  # n > 64
     assert L.tsqr_s_form_q(100, 8, a.data_ptr(), 99, w.data_ptr(), 1 << 20, None) == 1
+
+
+def test_implicit_with_padded_leading_dimensions(orc, cuda, tg):
+    """lda > m for the factored A, ldc > m for C and ldd > n for D."""
+    import torch
+    m, n, k = 30001, 24, 6
+    A0 = orc.fill_uniform(m, n, np.float32, seed=55)
+    C0 = orc.fill_uniform(m, k, np.float32, seed=56)
+    A = tg.empty_colmajor(m, n, torch.float32, "cuda", ld=m + 5)
+    A.copy_(torch.from_numpy(np.ascontiguousarray(A0)))
+    C = tg.empty_colmajor(m, k, torch.float32, "cuda", ld=m + 3)
+    C.copy_(torch.from_numpy(np.ascontiguousarray(C0)))
+    D = tg.empty_colmajor(n, k, torch.float32, "cuda", ld=n + 2)
+    fac = tg.factor_(A)
+    tg.apply_qt_(fac, C, D)
+    Q = to_dev(tg, A0)
+    tg.tsqr_(Q)
+    torch.cuda.synchronize()
+    ref = to_host(Q).astype(np.float64).T @ C0.astype(np.float64)
+    err = np.linalg.norm(to_host(D).astype(np.float64) - ref)
+    assert err <= 20 * n * 2.0 ** -24 * np.linalg.norm(C0.astype(np.float64)), err
+    tg.form_q_(fac)
+    torch.cuda.synchronize()
+    assert np.array_equal(to_host(A), to_host(Q))
