@@ -133,6 +133,21 @@ tsqr_status tsqr_batched_s(int count, float* const* A, const int64_t* m, const i
                            const int64_t* lda, float* const* R, const int64_t* ldr,
                            void* work, size_t work_bytes, const tsqr_opts* opts, void* stream);
 
+/* Autotuner of the batched form.  Each width class (0: n <= 8, 1: n <= 16,
+ * 2: n <= 32, 3: n <= 64) has candidate tile configurations (candidate 0 is
+ * the single-problem path's tile height, candidate 1 half of it), chosen per
+ * height bucket (0: m < 8192, 1: m < 65536, 2: m >= 65536) by a
+ * process-wide table that tsqr_batched_s reads once per call.
+ * tsqr_batched_tune_s times every candidate of each (class, bucket) present
+ * in the given shapes, on synthetic matrices of those shapes (reps timed
+ * runs after one warm-up), and keeps the fastest.  It allocates its own
+ * scratch, synchronizes, and must not run concurrently with batched calls.
+ * The workspace size of tsqr_batched_workspace_bytes holds for every choice. */
+tsqr_status tsqr_batched_tune_s(int count, const int64_t* m, const int64_t* n, int reps, void* stream);
+int tsqr_batched_choice(int width_class, int height_bucket);         /* -1 on bad arguments */
+int tsqr_batched_candidate_rows(int width_class, int candidate);     /* tile height, -1 on bad arguments */
+tsqr_status tsqr_batched_set_choice(int width_class, int height_bucket, int candidate);
+
 /* FP32 TSQR that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: frameworks that have already
  * reserved nearly all device memory for their own pool, programs with a

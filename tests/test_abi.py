@@ -165,3 +165,22 @@ def test_qr_algorithm_option(tg):
     assert L.qr_s_ex(1000, 64, fake, 1000, fake, 64, fake, 1 << 30, ctypes.byref(o), None) == 2
     o = tg._opts("plain", algorithm="householder")
     assert L.qr_s_ex(1000, 64, fake, 1000, fake, 64, fake, 16, ctypes.byref(o), None) == 3
+
+
+def test_batched_tuning_table_needs_no_gpu(tg):
+    """The autotuner's table: defaults, candidate tile heights, and argument
+    checks of the tuning and setting calls (no CUDA call)."""
+    L = tg.lib()
+    assert [L.tsqr_batched_candidate_rows(c, 0) for c in range(4)] == [1024, 512, 512, 512]
+    assert [L.tsqr_batched_candidate_rows(c, 1) for c in range(4)] == [512, 256, 256, 256]
+    assert L.tsqr_batched_candidate_rows(4, 0) == -1 and L.tsqr_batched_candidate_rows(0, 2) == -1
+    assert all(L.tsqr_batched_choice(c, b) == 0 for c in range(4) for b in range(3))
+    assert L.tsqr_batched_choice(0, 3) == -1
+    assert L.tsqr_batched_set_choice(2, 1, 1) == 0 and L.tsqr_batched_choice(2, 1) == 1
+    assert L.tsqr_batched_set_choice(2, 1, 0) == 0
+    assert L.tsqr_batched_set_choice(2, 1, 2) == 1 and L.tsqr_batched_set_choice(-1, 0, 0) == 1
+    i64 = ctypes.c_int64 * 2
+    assert L.tsqr_batched_tune_s(0, i64(100, 100), i64(8, 8), 3, None) == 1
+    assert L.tsqr_batched_tune_s(2, i64(100, 100), i64(8, 65), 3, None) == 1
+    assert L.tsqr_batched_tune_s(2, i64(100, 5), i64(8, 8), 3, None) == 1
+    assert L.tsqr_batched_tune_s(2, i64(100, 100), i64(8, 8), 0, None) == 1

@@ -107,3 +107,50 @@ def test_batch_argument_checks(cuda, tg):
     assert L.tsqr_batched_s(1, p, one(100), one(65), one(100), p, one(65), p, 1 << 20, None, None) == 2
     assert L.tsqr_batched_s(1, p, one(10), one(20), one(10), p, one(20), p, 1 << 20, None, None) == 1
     assert L.tsqr_batched_s(1, p, one(100), one(8), one(100), p, one(8), p, 1, None, None) == 3
+
+
+def _set_all(tg, cand):
+    for c in range(4):
+        for b in range(3):
+            assert tg.lib().tsqr_batched_set_choice(c, b, cand) == 0
+
+
+@pytest.mark.parametrize("cand", [0, 1])
+def test_every_tuning_candidate_meets_the_bar(orc, cuda, tg, cand):
+    """Each candidate tile configuration of the autotuner, forced for every
+    class and bucket, meets the plain-path parity bar (its tree differs from
+    the single-problem path's when the tile height differs)."""
+    import torch
+    _set_all(tg, cand)
+    try:
+        As = [orc.fill_uniform(m, n, np.float32, seed=300 + k) for k, (m, n) in enumerate(SHAPES)]
+        dAs = [dev(tg, A) for A in As]
+        dRs = tg.tsqr_batched_(dAs)
+        torch.cuda.synchronize()
+        u = 2.0 ** -24
+        for A, dA, dR in zip(As, dAs, dRs):
+            m, n = A.shape
+            met = orc.metrics(A, host(dA), host(dR))
+            assert met["backward"] <= 10 * n * u and met["orth"] <= 10 * n * u, (cand, m, n, met)
+    finally:
+        _set_all(tg, 0)
+
+
+def test_tuner_picks_valid_candidates_and_results_hold(orc, cuda, tg):
+    import torch
+    shapes = [(2048, 8), (5000, 16), (30000, 32), (100000, 64), (70000, 16), (3000, 32)]
+    try:
+        table = tg.batched_tune_(shapes, reps=2)
+        for (c, b), (k, rows) in table.items():
+            assert k in (0, 1) and rows == tg.lib().tsqr_batched_candidate_rows(c, k)
+        As = [orc.fill_uniform(m, n, np.float32, seed=400 + k) for k, (m, n) in enumerate(shapes)]
+        dAs = [dev(tg, A) for A in As]
+        dRs = tg.tsqr_batched_(dAs)
+        torch.cuda.synchronize()
+        u = 2.0 ** -24
+        for A, dA, dR in zip(As, dAs, dRs):
+            m, n = A.shape
+            met = orc.metrics(A, host(dA), host(dR))
+            assert met["backward"] <= 10 * n * u and met["orth"] <= 10 * n * u, (m, n, met)
+    finally:
+        _set_all(tg, 0)

@@ -19,7 +19,7 @@ import os
 
 __all__ = [
     "TsqrError", "PLAIN", "TF32X3", "BF16X3", "lib", "library_path", "tsqr", "qr", "tsqr_", "qr_",
-    "tsqr_batched_", "profile_", "check_", "factor_", "apply_qt_", "form_q_", "Factorization", "workspace_bytes",
+    "tsqr_batched_", "batched_tune_", "batched_table", "profile_", "check_", "factor_", "apply_qt_", "form_q_", "Factorization", "workspace_bytes",
     "qr_workspace_bytes", "empty_colmajor", "to_colmajor",
 ]
 
@@ -71,6 +71,10 @@ EXPORTS = {
     "tsqr_batched_s": ([ctypes.c_int, _p, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p],
                        ctypes.c_int),
     "tsqr_s_noalloc": ([_i64, _i64, _p, _i64, _p, _i64, _p], ctypes.c_int),
+    "tsqr_batched_tune_s": ([ctypes.c_int, _p, _p, ctypes.c_int, _p], ctypes.c_int),
+    "tsqr_batched_choice": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "tsqr_batched_candidate_rows": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "tsqr_batched_set_choice": ([ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "tsqr_host_workspace_bytes": ([_i64, _i64, ctypes.c_int, ctypes.POINTER(Opts)], ctypes.c_size_t),
     "tsqr_workspace_check": ([_p], ctypes.c_int),
     "tsqr_s_host": ([_i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, ctypes.c_size_t, ctypes.POINTER(Opts), _p],
@@ -383,6 +387,30 @@ def profile_(kind, A, R, precision="plain", reorth=False, panel=0, work=None, st
                               wb, ctypes.byref(o), _stream_handle(stream), ms, tags, max_launch,
                               ctypes.byref(cnt)), "profile_")
     return [(tags[i], ms[i]) for i in range(cnt.value)]
+
+
+def batched_tune_(shapes, reps=3, stream=None):
+    """Autotune the batched form for a list of (m, n) shapes: every candidate
+    tile configuration of each (width class, height bucket) present is timed
+    on synthetic matrices and the fastest kept (process-wide).  Returns the
+    table: {(class, bucket): (candidate, tile rows)}."""
+    count = len(shapes)
+    i64 = ctypes.c_int64 * count
+    m = i64(*[int(a) for a, _ in shapes])
+    n = i64(*[int(b) for _, b in shapes])
+    _check(lib().tsqr_batched_tune_s(count, m, n, int(reps), _stream_handle(stream)), "batched_tune_")
+    return batched_table()
+
+
+def batched_table():
+    """The batched form's current choices: {(class, bucket): (candidate, rows)}."""
+    L = lib()
+    out = {}
+    for c in range(4):
+        for b in range(3):
+            k = L.tsqr_batched_choice(c, b)
+            out[(c, b)] = (k, L.tsqr_batched_candidate_rows(c, k))
+    return out
 
 
 def tsqr_batched_(As, Rs=None, precision="plain", work=None, stream=None):

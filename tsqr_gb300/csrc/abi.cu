@@ -211,6 +211,19 @@ size_t tsqr_batched_workspace_bytes(int count, const int64_t* m, const int64_t* 
     return tsqr::batched_workspace(count, m, n);
 }
 
+tsqr_status tsqr_batched_tune_s(int count, const int64_t* m, const int64_t* n, int reps, void* stream) {
+    return tsqr::batched_tune(count, m, n, reps, (cudaStream_t)stream);
+}
+int tsqr_batched_choice(int width_class, int height_bucket) {
+    return tsqr::batched_choice(width_class, height_bucket);
+}
+int tsqr_batched_candidate_rows(int width_class, int candidate) {
+    return tsqr::batched_candidate_rows(width_class, candidate);
+}
+tsqr_status tsqr_batched_set_choice(int width_class, int height_bucket, int candidate) {
+    return tsqr::batched_set_choice(width_class, height_bucket, candidate);
+}
+
 tsqr_status tsqr_batched_s(int count, float* const* A, const int64_t* m, const int64_t* n, const int64_t* lda,
                            float* const* R, const int64_t* ldr, void* work, size_t work_bytes,
                            const tsqr_opts* opts, void* stream) {

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "internal.h"
@@ -29,6 +30,8 @@ namespace tsqr {
 namespace {
 
 constexpr int kTable = 448;  // descriptors per launch (fits the 32 KB parameter space)
+constexpr int kBatchedCands = 2;    // tile configurations per width class
+constexpr int kBatchedBuckets = 3;  // problem-height buckets of the tuning table
 
 struct FactorItem {
     float* M;
@@ -156,16 +159,35 @@ struct SplitCls {
     static ClassCfg cfg() { return {NMAX, 32 * RPT, MINB, AMINB, &factor, &class_apply<NMAX, 32 * RPT, ANT, AMINB>}; }
 };
 
-const ClassCfg& class_of(int n) {
-    static const ClassCfg c8 = Cls<8, 256, 4, 3, 3>::cfg();
-    static const ClassCfg c16 = SplitCls<16, 4, 16, 4, 3, 256>::cfg();
-    static const ClassCfg c32 = SplitCls<32, 4, 16, 2, 2, 256>::cfg();
-    static const ClassCfg c64 = SplitCls<64, 8, 16, 1, 1, 256>::cfg();
-    if (n <= 8) return c8;
-    if (n <= 16) return c16;
-    if (n <= 32) return c32;
-    return c64;
+// Candidate tile configurations per width class (n <= 8, 16, 32, 64).
+// Candidate 0 is the single-problem path's configuration; candidate 1 halves
+// the tile height (more tiles, hence more parallelism, for short problems,
+// at the cost of a taller stacked-R level).
+int class_index(int n) { return n <= 8 ? 0 : (n <= 16 ? 1 : (n <= 32 ? 2 : 3)); }
+
+const ClassCfg& candidate(int ci, int cand) {
+    static const ClassCfg c[4][kBatchedCands] = {
+        {Cls<8, 256, 4, 3, 3>::cfg(), Cls<8, 256, 2, 3, 3>::cfg()},
+        {SplitCls<16, 4, 16, 4, 3, 256>::cfg(), SplitCls<16, 4, 8, 4, 3, 256>::cfg()},
+        {SplitCls<32, 4, 16, 2, 2, 256>::cfg(), SplitCls<32, 4, 8, 2, 2, 256>::cfg()},
+        {SplitCls<64, 8, 16, 1, 1, 256>::cfg(), SplitCls<64, 8, 8, 1, 1, 256>::cfg()},
+    };
+    return c[ci][cand];
 }
+
+// Height bucket of a problem: m < 8192, m < 65536, m >= 65536.
+int bucket_of(int64_t m) { return m < 8192 ? 0 : (m < 65536 ? 1 : 2); }
+
+// The autotuner's table: candidate per (class, bucket), candidate 0 until a
+// tuning call or tsqr_batched_set_choice changes it.  Process-wide.
+std::mutex g_table_mu;
+int g_table[4][kBatchedBuckets] = {};
+
+int choice_of(int ci, int bk) {
+    std::lock_guard<std::mutex> g(g_table_mu);
+    return g_table[ci][bk];
+}
+
 
 struct Lvl {
     float* M;
@@ -203,11 +225,17 @@ int resident_grid(const ClassCfg& c, bool apply, int64_t tiles) {
 
 }  // namespace
 
+// Sized for the largest candidate of each problem, so the answer holds
+// whatever the tuning table says when the call runs.
 size_t batched_workspace(int count, const int64_t* m, const int64_t* n) {
     size_t total = 0;
     for (int i = 0; i < count; ++i) {
         if (m[i] < 1 || n[i] < 1 || n[i] > 64 || m[i] < n[i]) return 0;
-        total += tree_of(m[i], n[i], nullptr, m[i], class_of((int)n[i]).rows, nullptr, nullptr);
+        size_t most = 0;
+        for (int c = 0; c < kBatchedCands; ++c)
+            most = std::max(most, tree_of(m[i], n[i], nullptr, m[i], candidate(class_index((int)n[i]), c).rows,
+                                          nullptr, nullptr));
+        total += most;
     }
     return total < 256 ? 256 : total;
 }
@@ -218,23 +246,33 @@ tsqr_status batched_run(int count, float* const* A, const int64_t* m, const int6
     const size_t need = batched_workspace(count, m, n);
     if (need == 0) return TSQR_ERR_INVALID_ARG;
     if (work == nullptr || work_bytes < need) return TSQR_ERR_WORKSPACE;
+    // One snapshot of the tuning table for the whole call.
+    int table[4][kBatchedBuckets];
+    {
+        std::lock_guard<std::mutex> g(g_table_mu);
+        std::copy(&g_table[0][0], &g_table[0][0] + 4 * kBatchedBuckets, &table[0][0]);
+    }
+    std::vector<int> cand_of(count);
+    for (int i = 0; i < count; ++i) cand_of[i] = table[class_index((int)n[i])][bucket_of(m[i])];
     // Trees of every problem.
     std::vector<std::vector<Lvl>> trees(count);
     char* base = reinterpret_cast<char*>(work);
     size_t off = 0;
     for (int i = 0; i < count; ++i)
-        off += tree_of(m[i], n[i], A[i], lda[i], class_of((int)n[i]).rows, base + off, &trees[i]);
+        off += tree_of(m[i], n[i], A[i], lda[i], candidate(class_index((int)n[i]), cand_of[i]).rows, base + off,
+                       &trees[i]);
 
-    const int classes[4] = {8, 16, 32, 64};
     FactorTable* ft = new FactorTable;
     ApplyTable* at = new ApplyTable;
     tsqr_status st = TSQR_OK;
-    for (int ci = 0; ci < 4 && st == TSQR_OK; ++ci) {
+    // one group per (width class, candidate configuration)
+    for (int g = 0; g < 4 * kBatchedCands && st == TSQR_OK; ++g) {
+        const int ci = g / kBatchedCands, cand = g % kBatchedCands;
         std::vector<int> members;
         for (int i = 0; i < count; ++i)
-            if (class_of((int)n[i]).nmax == classes[ci]) members.push_back(i);
+            if (class_index((int)n[i]) == ci && cand_of[i] == cand) members.push_back(i);
         if (members.empty()) continue;
-        const ClassCfg& C = class_of(classes[ci]);
+        const ClassCfg& C = candidate(ci, cand);
         int maxL = 0;
         for (int i : members) maxL = std::max(maxL, (int)trees[i].size());
         // up-sweep: one launch per level (and per table of kTable problems)
@@ -294,6 +332,109 @@ tsqr_status batched_run(int count, float* const* A, const int64_t* m, const int6
     delete ft;
     delete at;
     return st;
+}
+
+namespace {
+
+__global__ void fill_uniform_kernel(float* a, int64_t count, uint32_t seed) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t x = (uint32_t)i * 2654435761u ^ (uint32_t)(i >> 32) ^ seed;
+        x ^= x >> 15;
+        x *= 2246822519u;
+        x ^= x >> 13;
+        a[i] = (float)(x >> 8) * (2.0f / 16777216.0f) - 1.0f;
+    }
+}
+
+}  // namespace
+
+// Times every candidate configuration of each (width class, height bucket)
+// present in the given shapes on synthetic matrices of those shapes, and
+// keeps the fastest in the table.  Allocates its own scratch.
+tsqr_status batched_tune(int count, const int64_t* m, const int64_t* n, int reps, cudaStream_t s) {
+    if (count < 1 || !m || !n || reps < 1) return TSQR_ERR_INVALID_ARG;
+    for (int i = 0; i < count; ++i)
+        if (m[i] < 1 || n[i] < 1 || n[i] > 64 || m[i] < n[i] || m[i] > INT32_MAX) return TSQR_ERR_INVALID_ARG;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return TSQR_ERR_CUDA;
+    tsqr_status st = TSQR_OK;
+    for (int ci = 0; ci < 4 && st == TSQR_OK; ++ci)
+        for (int bk = 0; bk < kBatchedBuckets && st == TSQR_OK; ++bk) {
+            std::vector<int64_t> mm, nn, ld, ldr;
+            for (int i = 0; i < count; ++i)
+                if (class_index((int)n[i]) == ci && bucket_of(m[i]) == bk) {
+                    mm.push_back(m[i]);
+                    nn.push_back(n[i]);
+                }
+            if (mm.empty()) continue;
+            const int k = (int)mm.size();
+            int64_t elems = 0, relems = 0;
+            for (int i = 0; i < k; ++i) elems += mm[i] * nn[i], relems += nn[i] * nn[i];
+            const size_t wb = batched_workspace(k, mm.data(), nn.data());
+            float *dA = nullptr, *dR = nullptr;
+            void* dW = nullptr;
+            if (cudaMalloc(&dA, sizeof(float) * elems) != cudaSuccess ||
+                cudaMalloc(&dR, sizeof(float) * relems) != cudaSuccess || cudaMalloc(&dW, wb) != cudaSuccess) {
+                st = TSQR_ERR_CUDA;
+            } else {
+                std::vector<float*> pa(k), pr(k);
+                int64_t oa = 0, orr = 0;
+                for (int i = 0; i < k; ++i) {
+                    pa[i] = dA + oa;
+                    pr[i] = dR + orr;
+                    oa += mm[i] * nn[i];
+                    orr += nn[i] * nn[i];
+                    ld.push_back(mm[i]);
+                    ldr.push_back(nn[i]);
+                }
+                int best = 0;
+                float best_ms = 0.f;
+                for (int cand = 0; cand < kBatchedCands && st == TSQR_OK; ++cand) {
+                    {
+                        std::lock_guard<std::mutex> g(g_table_mu);
+                        g_table[ci][bk] = cand;
+                    }
+                    float total = 0.f;
+                    for (int r = 0; r <= reps && st == TSQR_OK; ++r) {  // r = 0 is a warm-up
+                        fill_uniform_kernel<<<1024, 256, 0, s>>>(dA, elems, 977u * (uint32_t)(r + 1));
+                        cudaEventRecord(e0, s);
+                        st = batched_run(k, pa.data(), mm.data(), nn.data(), ld.data(), pr.data(), ldr.data(), dW, wb,
+                                         s);
+                        cudaEventRecord(e1, s);
+                        if (st == TSQR_OK && cudaEventSynchronize(e1) != cudaSuccess) st = TSQR_ERR_CUDA;
+                        float ms = 0.f;
+                        if (st == TSQR_OK && r > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) total += ms;
+                    }
+                    if (st == TSQR_OK && (cand == 0 || total < best_ms)) best = cand, best_ms = total;
+                }
+                std::lock_guard<std::mutex> g(g_table_mu);
+                g_table[ci][bk] = best;
+            }
+            cudaFree(dA);
+            cudaFree(dR);
+            cudaFree(dW);
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return st;
+}
+
+int batched_choice(int ci, int bk) {
+    if (ci < 0 || ci >= 4 || bk < 0 || bk >= kBatchedBuckets) return -1;
+    return choice_of(ci, bk);
+}
+
+int batched_candidate_rows(int ci, int cand) {
+    if (ci < 0 || ci >= 4 || cand < 0 || cand >= kBatchedCands) return -1;
+    return candidate(ci, cand).rows;
+}
+
+tsqr_status batched_set_choice(int ci, int bk, int cand) {
+    if (ci < 0 || ci >= 4 || bk < 0 || bk >= kBatchedBuckets || cand < 0 || cand >= kBatchedCands)
+        return TSQR_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(g_table_mu);
+    g_table[ci][bk] = cand;
+    return TSQR_OK;
 }
 
 }  // namespace tsqr

@@ -91,6 +91,10 @@ void tc_gemm_nn(int64_t M, int N, int K, float alpha, const float* A, int64_t ld
 namespace tsqr {
 // Batched TSQR (batched.cu), FP32, n <= 64.
 size_t batched_workspace(int count, const int64_t* m, const int64_t* n);
+tsqr_status batched_tune(int count, const int64_t* m, const int64_t* n, int reps, cudaStream_t s);
+int batched_choice(int width_class, int height_bucket);
+int batched_candidate_rows(int width_class, int candidate);
+tsqr_status batched_set_choice(int width_class, int height_bucket, int candidate);
 tsqr_status batched_run(int count, float* const* A, const int64_t* m, const int64_t* n, const int64_t* lda,
                         float* const* R, const int64_t* ldr, void* work, size_t work_bytes, cudaStream_t s);
 }  // namespace tsqr
