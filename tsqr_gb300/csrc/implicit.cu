@@ -256,8 +256,10 @@ __global__ void __launch_bounds__(kNT) apply_qt_column(QtParams<T, NMAX> p, int6
 
 template <typename T, int NMAX>
 cudaError_t launch_apply_qt(const QtParams<T, NMAX>& p, cudaStream_t s) {
-    if (p.k <= 4 && p.rows <= 4 * kNT) {
-        // a few columns: one streaming pass per column
+    if (p.k <= 2 && p.rows <= 4 * kNT) {
+        // one or two columns: one streaming pass per column (about 0.28 ms
+        // each at 4,194,304 x 32, against about 0.75 ms for the blocked
+        // kernel at any k up to 32)
         static int sms = 0;
         if (!sms) {
             int dev = 0;
