@@ -58,9 +58,10 @@ def test_precision_form_ill_conditioned(orc, cuda, tg, kappa):
     assert met["backward"] <= 1e-5 and met["orth"] <= 1e-5, met
 
 
-def test_precision_form_full_size(cuda, tg):
+@pytest.mark.parametrize("n", [32, 64])
+def test_precision_form_full_size(cuda, tg, n):
     import torch
-    m, n = 4194304, 32
+    m = 4194304
     g = torch.Generator(device="cuda").manual_seed(6)
     A0 = torch.rand((n, m), generator=g, device="cuda").mul_(2).sub_(1).t()
     A = A0.t().clone().t()

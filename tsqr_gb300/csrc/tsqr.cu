@@ -335,10 +335,11 @@ tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R
             if (!tc_apply_level(ap, c.nmax, c.rows, err, s)) return TSQR_ERR_UNSUPPORTED;
             log_launch(kTagTc + l, s);
         } else {
-            // 32 < n <= 64: the per-tile W = T (V_top^T B) setup is O(n^3) on
-            // CUDA cores for every 256-row tile and outweighs what the tensor
-            // cores save on V W (measured 7.0 ms vs 4.0 ms for the level-0
-            // apply at 4,194,304 x 64), so the CUDA-core apply runs instead.
+            // 32 < n <= 64: the CUDA-core apply runs instead.  The tensor-core
+            // apply at 64 columns needs 132 KB of shared memory and 247
+            // registers, so one CTA of 4 warps per SM, which cannot hide its
+            // O(n^3) W products and per-block chain: the whole call at
+            // 4,194,304 x 64 took 6.98 ms with it against 6.42 ms with this.
             constexpr int ve = 4;
             ap.vec = (lv[l].ld % ve == 0 && (reinterpret_cast<uintptr_t>(lv[l].M) % 16) == 0) ? 1 : 0;
             c.ks.apply(ap, (int)std::min<int64_t>(lv[l].ntiles, 1 << 30), s);
