@@ -133,11 +133,11 @@ template <int NMAX, int B, int ANT, int AMINB>
 void class_apply(const ApplyTable& t, int grid, cudaStream_t s) {
     constexpr int ARPT = B / ANT;  // the apply CTA covers the tile height
     constexpr size_t kSmem = apply_smem_bytes<float, NMAX, B>();
-    static bool attr = [] {
-        return cudaFuncSetAttribute(batched_apply<NMAX, ANT, ARPT, AMINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kSmem) == cudaSuccess;
-    }();
-    (void)attr;
+    static PerDeviceOnce attr;
+    attr.run([] {
+        cudaFuncSetAttribute(batched_apply<NMAX, ANT, ARPT, AMINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kSmem);
+    });
     batched_apply<NMAX, ANT, ARPT, AMINB><<<grid, ANT, kSmem, s>>>(t);
 }
 
@@ -212,13 +212,7 @@ size_t tree_of(int64_t m, int64_t n, float* A, int64_t lda, int rows, char* base
 }
 
 int resident_grid(const ClassCfg& c, bool apply, int64_t tiles) {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 148;
-    }
+    const int sms = device_sm_count();
     const int per_sm = apply ? c.apply_per_sm : c.factor_per_sm;
     return (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * per_sm));
 }

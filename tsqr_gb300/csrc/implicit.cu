@@ -260,20 +260,20 @@ cudaError_t launch_apply_qt(const QtParams<T, NMAX>& p, cudaStream_t s) {
         // one or two columns: one streaming pass per column (about 0.28 ms
         // each at 4,194,304 x 32, against about 0.75 ms for the blocked
         // kernel at any k up to 32)
-        static int sms = 0;
-        if (!sms) {
-            int dev = 0;
-            cudaGetDevice(&dev);
-            if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 148;
-        }
+        const int sms = device_sm_count();
         const int grid = (int)std::min<int64_t>(p.ntiles, (int64_t)sms * 8);
         for (int64_t c = 0; c < p.k; ++c) apply_qt_column<T, NMAX><<<grid, kNT, 0, s>>>(p, c);
         return cudaGetLastError();
     }
     constexpr size_t smem = sizeof(QtSmem<T, NMAX>);
-    static const bool attr = cudaFuncSetAttribute(apply_qt_tiles<T, NMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)smem) == cudaSuccess;
-    if (!attr) return cudaErrorInvalidValue;
+    // a failure shows here on the device's first call, and in the launch
+    // error of every later one
+    cudaError_t attr = cudaSuccess;
+    static PerDeviceOnce attr_once;
+    attr_once.run([&] {
+        attr = cudaFuncSetAttribute(apply_qt_tiles<T, NMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
+    if (attr != cudaSuccess) return attr;
     const int64_t items = p.ntiles * ((p.k + kKB - 1) / kKB);
     const int grid = (int)std::min<int64_t>(items, 1 << 20);
     apply_qt_tiles<T, NMAX><<<grid, kNT, smem, s>>>(p);

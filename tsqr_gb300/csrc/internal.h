@@ -4,11 +4,64 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <atomic>
+#include <mutex>
 #include <vector>
 
 #include "../../include/tsqr_gb300.h"
 
 namespace tsqr {
+
+// Function attributes (the dynamic shared-memory limit) and device
+// properties belong to one device's context, so the caches below keep one
+// entry per device: a process that drives several GPUs sets each one up.
+constexpr int kMaxDevices = 64;
+
+inline int current_device() {
+    int dev = 0;
+    return cudaGetDevice(&dev) == cudaSuccess ? dev : 0;
+}
+
+// Runs f() once per device (the current device at the call); thread-safe.
+// Devices past kMaxDevices are not cached: f() runs on every call.
+class PerDeviceOnce {
+  public:
+    template <typename F>
+    void run(F&& f) {
+        const int dev = current_device();
+        if (dev < 0 || dev >= kMaxDevices) {
+            f();
+            return;
+        }
+        const uint64_t bit = 1ull << dev;
+        if (done_.load(std::memory_order_acquire) & bit) return;
+        std::lock_guard<std::mutex> lk(mu_);
+        if (done_.load(std::memory_order_relaxed) & bit) return;
+        f();
+        done_.fetch_or(bit, std::memory_order_release);
+    }
+
+  private:
+    std::atomic<uint64_t> done_{0};
+    std::mutex mu_;
+};
+
+// Streaming multiprocessors of the current device, cached per device (148
+// if the attribute cannot be read; the launch that follows then reports the
+// error).
+inline int device_sm_count() {
+    static std::atomic<int> cache[kMaxDevices];
+    const int dev = current_device();
+    const bool cached = dev >= 0 && dev < kMaxDevices;
+    if (cached) {
+        const int v = cache[dev].load(std::memory_order_relaxed);
+        if (v > 0) return v;
+    }
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 148;
+    if (cached) cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
 
 // Launch log for the instrumented entry point: when active on this host
 // thread, every kernel launch of the library records a CUDA event after it

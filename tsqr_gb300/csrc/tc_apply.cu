@@ -255,11 +255,10 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
 template <int NMAX, int B>
 void launch(const ApplyParams<float>& p, int grid, int* err, cudaStream_t s) {
     constexpr size_t smem = sizeof(TcApplySmem<NMAX>) + 1024;
-    static bool attr = [] {
-        return cudaFuncSetAttribute(tc_apply_tiles<NMAX, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem) == cudaSuccess;
-    }();
-    (void)attr;
+    static PerDeviceOnce attr;
+    attr.run([] {
+        cudaFuncSetAttribute(tc_apply_tiles<NMAX, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
     tc_apply_tiles<NMAX, B><<<grid, 128, smem, s>>>(p, err);
 }
 
@@ -268,12 +267,7 @@ void launch(const ApplyParams<float>& p, int grid, int* err, cudaStream_t s) {
 // Tile heights must match the factor configuration of the precision path.
 bool tc_apply_level(const ApplyParams<float>& p, int nmax, int rows, int* err, cudaStream_t s) {
     // persistent grid: resident CTAs walk the tiles, prefetching the next one
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 148;
-    }
+    const int sms = device_sm_count();
     const int64_t resident = (int64_t)sms * (nmax <= 32 ? 4 : 1);
     const int grid = (int)(p.ntiles < 1 ? 1 : (p.ntiles > resident ? resident : p.ntiles));
     if (nmax == 32 && rows == 512) {

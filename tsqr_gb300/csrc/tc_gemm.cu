@@ -268,11 +268,10 @@ template <bool TRANS_A, int NB>
 void launch_gemm(dim3 grid, int M, int N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
                  float* C, int64_t ldc, float alpha, int64_t kchunk, int* err, cudaStream_t s) {
     constexpr size_t smem = sizeof(GemmSmem<NB>) + 1024;
-    static bool attr = [] {
-        return cudaFuncSetAttribute(tc_gemm_kernel<TRANS_A, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem) == cudaSuccess;
-    }();
-    (void)attr;
+    static PerDeviceOnce attr;
+    attr.run([] {
+        cudaFuncSetAttribute(tc_gemm_kernel<TRANS_A, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
     tc_gemm_kernel<TRANS_A, NB><<<grid, 128, smem, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err);
 }
 

@@ -33,11 +33,11 @@ struct TileCfg {
     }
     static void apply(const ApplyParams<T>& p, int grid, cudaStream_t s) {
         constexpr size_t smem = apply_smem_bytes<T, NMAX, ANT * ARPT>();
-        static bool attr = [] {
-            return cudaFuncSetAttribute(apply_tiles<T, NMAX, ANT, ARPT, AMINB>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
-        }();
-        (void)attr;
+        static PerDeviceOnce attr;
+        attr.run([] {
+            cudaFuncSetAttribute(apply_tiles<T, NMAX, ANT, ARPT, AMINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+        });
         apply_tiles<T, NMAX, ANT, ARPT, AMINB><<<grid, ANT, smem, s>>>(p);
     }
 };
