@@ -71,6 +71,11 @@ def build_lib(force=False, verbose=False):
             cmd = [nvcc()] + ARCH + NVFLAGS + ["-I", INCLUDE, "-c", src, "-o", obj]
             jobs.append(ex.submit(_run, cmd))
         logs = [j.result() for j in jobs]
+    # ptxas's spill report of each unit (-warn-spills), read by the build
+    # hygiene test
+    for s, l in zip(SOURCES, logs):
+        with open(os.path.join(BUILD, s.replace(".cu", ".ptxas.log")), "w") as f:
+            f.write(l)
     if verbose:
         for l in logs:
             if l.strip():
