@@ -115,9 +115,15 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
+        return self.summarize(self.lines)
+
+    @staticmethod
+    def summarize(lines):
+        """Median SM clock, max clock and the throttle reasons seen Active in
+        csv,noheader,nounits lines of the query Q."""
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in self.lines:
+        for l in lines:
             f = [x.strip() for x in l.split(",")]
             if len(f) < 9:
                 continue

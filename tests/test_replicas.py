@@ -97,3 +97,4 @@ def test_reference_arm_torchrun_ws2_prints_one_line(orc):
     assert d["value"] > 0 and d["unit"] == "TFLOP/s" and d["higher_is_better"] is True
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
