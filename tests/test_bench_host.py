@@ -19,3 +19,12 @@ def test_clock_summary_reads_throttle_reasons():
     assert c["reasons"] == ["sw_power_cap"]
     hot = ["0, 1500, 2070, 1400.0, 0x0000000000000048, Active, Not Active, Active, Not Active"]
     assert bench.ClockSampler.summarize(hot)["reasons"] == ["hw_slowdown", "sw_thermal_slowdown"]
+
+
+def test_lapack_context_figure_lists_both_libraries():
+    sys.path.insert(0, ROOT)
+    import bench
+    c = bench.cpu_lapack(8192, 32)
+    assert c["value"] > 0 and c["unit"] == "TFLOP/s" and c["cores"] >= 1
+    assert len(c["candidates"]) == 2 and c["kind"] in c["candidates"]
+    assert c["seconds"] == min(v for v in c["candidates"].values() if isinstance(v, float))
