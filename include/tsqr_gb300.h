@@ -32,7 +32,7 @@ extern "C" {
 typedef enum tsqr_status {
     TSQR_OK = 0,
     TSQR_ERR_INVALID_ARG = 1,   /* bad m, n, lda, ldr, null pointer, m < n  */
-    TSQR_ERR_UNSUPPORTED = 2,   /* size or option this build does not cover */
+    TSQR_ERR_UNSUPPORTED = 2,   /* size or option the library does not cover */
     TSQR_ERR_WORKSPACE = 3,     /* workspace pointer null or too small      */
     TSQR_ERR_CUDA = 4,          /* a CUDA runtime call or launch failed     */
     TSQR_ERR_NO_DEVICE = 5      /* no CUDA device / wrong architecture      */
