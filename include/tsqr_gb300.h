@@ -160,7 +160,9 @@ tsqr_status tsqr_batched_set_choice(int width_class, int height_bucket, int cand
  * (tsqr_workspace_bytes) exceeds that size return TSQR_ERR_WORKSPACE
  * without launching (with n = 32, up to about 1.9 million rows fit).
  * The first call on a device looks up the array's device address with that
- * device current; make it before any stream capture.  All calls on a
+ * device current; make it before any stream capture.  Later calls repeat the
+ * lookup whenever their stream is not capturing (after a cudaDeviceReset
+ * the array may sit at a new address).  All calls on a
  * device share the array: calls that overlap on the GPU race, so the caller
  * must order them (one stream, or explicit synchronisation). */
 #define TSQR_NOALLOC_SCRATCH_BYTES (16u << 20)
@@ -237,6 +239,17 @@ const char* tsqr_status_string(tsqr_status s);
 
 /* Library version, e.g. "0.1.0". */
 const char* tsqr_version(void);
+
+/* Test hook for the failure path of the tensor-core kernels (no counterpart
+ * in the reference, whose grid barrier spins without a limit,
+ * kernelQR.h:374).  Sets how many times the tcgen05 kernels of later calls
+ * (tc_apply_tiles, tc_gemm_kernel) poll an mbarrier for their MMAs before
+ * giving up; 0 makes the first wait of every such kernel give up at once, so
+ * the call's status word is set and tsqr_workspace_check reports
+ * TSQR_ERR_CUDA.  The waits that let in-flight MMAs retire before TMEM is
+ * freed always keep the full limit.  polls < 0 restores the default
+ * (2^24 polls, seconds).  Process-wide; for tests only. */
+tsqr_status tsqr_debug_set_wait_limit(int polls);
 
 #ifdef __cplusplus
 }

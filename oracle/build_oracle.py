@@ -18,7 +18,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REF_SRC_DEFAULT = "/root/reference"
+# The reference checkout: TSQR_REFERENCE_SRC, or --ref-src on the command
+# line, else the checkout's location in the build container.
+REF_SRC_DEFAULT = os.environ.get("TSQR_REFERENCE_SRC", "/root/reference")
 
 
 def _newer(target, sources):
@@ -85,12 +87,18 @@ def build_ref_launcher(force=False):
     return out
 
 
-def build_all(force=False):
+def build_all(force=False, ref_src=None):
     paths = {"oracle": build_oracle(force)}
-    paths["ref_cubin"] = build_ref_cubin(force=force)
+    paths["ref_cubin"] = build_ref_cubin(ref_src or REF_SRC_DEFAULT, force=force)
     paths["ref_launch"] = build_ref_launcher(force)
     return paths
 
 
 if __name__ == "__main__":
-    print(build_all(force="--force" in sys.argv))
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--ref-src", default=None, help="the reference checkout (default: TSQR_REFERENCE_SRC or "
+                                                    "the build container's checkout)")
+    a = ap.parse_args()
+    print(build_all(force=a.force, ref_src=a.ref_src))

@@ -14,7 +14,7 @@ kernels from the cubin), and stores a small fixture:
   q_colsum         FP64 column sums of the full Q
   m, n, kind, dtype
 Fixtures are compared with the oracle restatement (CPU, test_golden.py) and
-with libtsqr_gb300 (GPU, test_golden_gpu.py).
+with libtsqr_gb300 (GPU, test_tsqr_gpu.py::test_matches_reference_cuda_golden).
 """
 import os
 import sys

@@ -184,3 +184,18 @@ def test_batched_tuning_table_needs_no_gpu(tg):
     assert L.tsqr_batched_tune_s(2, i64(100, 100), i64(8, 65), 3, None) == 1
     assert L.tsqr_batched_tune_s(2, i64(100, 5), i64(8, 8), 3, None) == 1
     assert L.tsqr_batched_tune_s(2, i64(100, 100), i64(8, 8), 0, None) == 1
+
+
+def test_noalloc_rejects_bad_arguments_before_any_cuda_call(tg):
+    """tsqr_s_noalloc checks its arguments first, like the other entry points:
+    n > 64 is unsupported; null matrices, short leading dimensions and m < n
+    are invalid.  Nothing is launched, so fake pointers are enough."""
+    fn = tg.lib().tsqr_s_noalloc
+    fake = ctypes.c_void_p(0x1000)
+    assert fn(1000, 65, fake, 1000, fake, 65, None) == 2   # TSQR_ERR_UNSUPPORTED
+    assert fn(1000, 32, None, 1000, fake, 32, None) == 1   # A null
+    assert fn(1000, 32, fake, 1000, None, 32, None) == 1   # R null
+    assert fn(1000, 32, fake, 999, fake, 32, None) == 1    # lda < m
+    assert fn(1000, 32, fake, 1000, fake, 31, None) == 1   # ldr < n
+    assert fn(16, 32, fake, 16, fake, 32, None) == 1       # m < n
+    assert fn(0, 32, fake, 1, fake, 32, None) == 1         # empty

@@ -1,6 +1,6 @@
-"""GPU tests of the precision form (TSQR_PRECISION_TF32X3): FP32 tile
-factorisation with FP64 norm/beta/tau, FP64 root combine, and every Q
-assembly on the tcgen05 tensor cores in TF32 hi/lo three-product form.
+"""GPU tests of the precision form (TSQR_PRECISION_TF32X3): the FP32 tile
+factorisation on CUDA cores, and every Q assembly on the tcgen05 tensor
+cores in TF32 hi/lo three-product form.
 
 Bar (the precision form's stated target): backward error and orthogonality
 <= 1e-5 against the FP64 oracle, for every result; R within 1e-5 max|R| of
@@ -161,3 +161,41 @@ def test_workspace_status_word_is_clear_after_tensor_core_calls(orc, cuda, tg):
     tg.tsqr_host_(hA, precision="tf32x3", work=w3)
     torch.cuda.synchronize()
     assert tg.lib().tsqr_workspace_check(w3.data_ptr()) == 0
+
+
+def test_a_tensor_core_wait_that_runs_out_is_reported_and_the_next_call_succeeds(orc, cuda, tg):
+    """Failure detection of the tcgen05 kernels, made to happen on purpose:
+    with their MMA waits limited to 0 polls (tsqr_debug_set_wait_limit), the
+    first wait of every tensor-core kernel gives up; the kernel lets its
+    in-flight MMAs retire (that wait keeps the full limit), frees its TMEM and
+    returns, and the call's status word reads TSQR_ERR_CUDA.  Nothing is left
+    broken: with the default limit restored the same calls succeed, clear the
+    word and meet the form's bar (<= 1e-5)."""
+    import torch
+    L = tg.lib()
+    m, n = 70000, 32
+    A = orc.fill_uniform(m, n, np.float32, seed=21)
+    m2, n2 = 20000, 256
+    B = orc.fill_uniform(m2, n2, np.float32, seed=22)
+    w = torch.zeros(tg.workspace_bytes(m, n, torch.float32, precision="tf32x3"), dtype=torch.uint8, device="cuda")
+    w2 = torch.zeros(tg.qr_workspace_bytes(m2, n2, torch.float32, precision="tf32x3"), dtype=torch.uint8,
+                     device="cuda")
+    try:
+        assert L.tsqr_debug_set_wait_limit(0) == 0
+        tg.tsqr_(to_dev(tg, A), precision="tf32x3", work=w)        # tc_apply_tiles
+        tg.qr_(to_dev(tg, B), precision="tf32x3", work=w2)         # tc_gemm_kernel
+        torch.cuda.synchronize()
+        assert L.tsqr_workspace_check(w.data_ptr()) == 4           # TSQR_ERR_CUDA
+        assert L.tsqr_workspace_check(w2.data_ptr()) == 4
+    finally:
+        L.tsqr_debug_set_wait_limit(-1)
+    torch.cuda.synchronize()                                        # the context is still usable
+    dA, dB = to_dev(tg, A), to_dev(tg, B)
+    dR = tg.tsqr_(dA, precision="tf32x3", work=w)
+    dR2 = tg.qr_(dB, precision="tf32x3", work=w2)
+    torch.cuda.synchronize()
+    assert L.tsqr_workspace_check(w.data_ptr()) == 0
+    assert L.tsqr_workspace_check(w2.data_ptr()) == 0
+    for M0, dQ, dRr in ((A, dA, dR), (B, dB, dR2)):
+        met = orc.metrics(M0, to_host(dQ), to_host(dRr))
+        assert met["backward"] <= 1e-5 and met["orth"] <= 1e-5, met

@@ -97,6 +97,7 @@ EXPORTS = {
                     ctypes.c_size_t, _p, ctypes.POINTER(CheckResult)], ctypes.c_int),
     "tsqr_status_string": ([ctypes.c_int], ctypes.c_char_p),
     "tsqr_version": ([], ctypes.c_char_p),
+    "tsqr_debug_set_wait_limit": ([ctypes.c_int], ctypes.c_int),
 }
 
 

@@ -82,7 +82,7 @@ def build_lib(force=False, verbose=False):
                 print(l)
     tmp = LIB + ".tmp"
     _run([nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", tmp] + objs +
-         ["-Xlinker", "-rpath,/usr/local/cuda/lib64", "-lcuda"])
+         ["-Xlinker", "-rpath,/usr/local/cuda/lib64"])
     os.replace(tmp, LIB)
     return LIB
 

@@ -257,6 +257,11 @@ const char* tsqr_status_string(tsqr_status s) {
 
 const char* tsqr_version(void) { return "0.1.0"; }
 
+tsqr_status tsqr_debug_set_wait_limit(int polls) {
+    tsqr::wait_tries().store(polls < 0 ? tsqr::kDefaultWaitTries : polls, std::memory_order_relaxed);
+    return TSQR_OK;
+}
+
 tsqr_status tsqr_profile(int kind, int elem_bytes, int64_t m, int64_t n, void* A, int64_t lda, void* R, int64_t ldr,
                          void* work, size_t work_bytes, const tsqr_opts* opts, void* stream, float* launch_ms,
                          int* launch_tag, int max_launch, int* n_launch) {

@@ -63,6 +63,16 @@ inline int device_sm_count() {
     return v;
 }
 
+// Polls allowed to the in-loop MMA waits of the tensor-core kernels
+// (tc_apply_tiles, tc_gemm_kernel); their clean-up waits before TMEM is
+// freed always keep the full limit.  Lowered only by the test entry point
+// tsqr_debug_set_wait_limit, to make a wait run out on purpose.
+constexpr int kDefaultWaitTries = 1 << 24;
+inline std::atomic<int>& wait_tries() {
+    static std::atomic<int> v{kDefaultWaitTries};
+    return v;
+}
+
 // Launch log for the instrumented entry point: when active on this host
 // thread, every kernel launch of the library records a CUDA event after it
 // on the launch stream, so per-launch device times can be read back.

@@ -22,9 +22,12 @@
 //     written earlier in the same call;
 //   * host code may not use the array's name as a device address (on the
 //     host it names a stand-in); the device address comes from
-//     cudaGetSymbolAddress, taken once per device, with that device
-//     current, on the first call made on the device.  Make that first call
-//     before any stream capture.
+//     cudaGetSymbolAddress, with the device current.  The first call made on
+//     a device takes it (this may load the library's device code), so make
+//     that first call before any stream capture.  Later calls look it up
+//     again whenever their stream is not capturing -- after a
+//     cudaDeviceReset the array may sit at a new address -- and a call on a
+//     capturing stream uses the address of the last such lookup.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -40,13 +43,18 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_scratch_ptr[kMaxDevices] = {nullptr};
 
-// Device address of g_noalloc_scratch on the current device (set-up on the
-// first call per device).
-tsqr_status scratch_address(void** out) {
+// Device address of g_noalloc_scratch on the current device: looked up
+// when the call's stream is not capturing (and on the first call of the
+// device), otherwise the last address looked up.
+tsqr_status scratch_address(cudaStream_t s, void** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TSQR_ERR_NO_DEVICE;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const bool query_failed = cudaStreamIsCapturing(s, &cap) != cudaSuccess;
+    if (query_failed) (void)cudaGetLastError();  // the failed query's own error only
+    const bool capturing = query_failed || cap != cudaStreamCaptureStatusNone;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (g_scratch_ptr[dev] == nullptr) {
+    if (g_scratch_ptr[dev] == nullptr || !capturing) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return TSQR_ERR_CUDA;
         g_scratch_ptr[dev] = p;
@@ -65,7 +73,7 @@ extern "C" tsqr_status tsqr_s_noalloc(int64_t m, int64_t n, float* A, int64_t ld
     if (need == 0) return TSQR_ERR_UNSUPPORTED;
     if (need > (size_t)TSQR_NOALLOC_SCRATCH_BYTES) return TSQR_ERR_WORKSPACE;
     void* scratch = nullptr;
-    tsqr_status st = scratch_address(&scratch);
+    tsqr_status st = scratch_address((cudaStream_t)stream, &scratch);
     if (st != TSQR_OK) return st;
     return tsqr::tsqr_plain<float>(m, n, A, lda, R, ldr, scratch, (size_t)TSQR_NOALLOC_SCRATCH_BYTES,
                                    (cudaStream_t)stream);

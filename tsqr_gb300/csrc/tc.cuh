@@ -102,11 +102,12 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
 
 // Bounded wait for phase `parity` of an mbarrier.  Each try_wait may suspend
-// the thread for a hardware-defined time; after kMbarTries unsuccessful tries
-// (seconds) it gives up and returns false instead of spinning forever.
+// the thread for a hardware-defined time; after `tries` unsuccessful tries
+// (kMbarTries: seconds) it gives up and returns false instead of spinning
+// forever.  tries = 0 gives up at once.
 constexpr int kMbarTries = 1 << 24;
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    for (int it = 0; it < kMbarTries; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, int tries = kMbarTries) {
+    for (int it = 0; it < tries; ++it) {
         uint32_t ok;
         asm volatile(
             "{\n"

@@ -50,7 +50,7 @@ struct TcApplySmem {
 };
 
 template <int NMAX, int B>
-__global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyParams<float> p, int* err) {
+__global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyParams<float> p, int* err, int tries) {
     static_assert(NMAX % 16 == 0 && NMAX <= 256 && B % 128 == 0, "bad shape");
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     TcApplySmem<NMAX>& S = *reinterpret_cast<TcApplySmem<NMAX>*>(tc_smem_raw);
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
                 load_block(t, blk + 1, vnext);
             else if (t + gridDim.x < p.ntiles)
                 load_block(t + gridDim.x, 0, vnext);
-            const bool waited = tc::mbar_wait(mbar, phase);
+            const bool waited = tc::mbar_wait(mbar, phase, tries);
             // a timed-out wait anywhere stops the whole CTA (uniform decision)
             if (__syncthreads_or(!waited)) {
                 ok = false;
@@ -259,7 +259,7 @@ void launch(const ApplyParams<float>& p, int grid, int* err, cudaStream_t s) {
     attr.run([] {
         cudaFuncSetAttribute(tc_apply_tiles<NMAX, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
-    tc_apply_tiles<NMAX, B><<<grid, 128, smem, s>>>(p, err);
+    tc_apply_tiles<NMAX, B><<<grid, 128, smem, s>>>(p, err, wait_tries().load(std::memory_order_relaxed));
 }
 
 }  // namespace

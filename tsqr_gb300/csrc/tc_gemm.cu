@@ -47,7 +47,7 @@ template <bool TRANS_A, int NB>
 __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, const float* __restrict__ A, int64_t lda,
                                                       const float* __restrict__ Bm, int64_t ldb, float* __restrict__ C,
                                                       int64_t ldc,
-                                                      float alpha, int64_t kchunk, int* err) {
+                                                      float alpha, int64_t kchunk, int* err, int tries) {
     extern __shared__ __align__(1024) unsigned char gemm_smem_raw[];
     GemmSmem<NB>& S = *reinterpret_cast<GemmSmem<NB>*>(gemm_smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -186,6 +186,20 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
         tc::mma_commit(tc::smem_u32(&S.mbar[buf]));
     };
 
+    // pend: buffers whose committed MMA group this thread has not yet seen
+    // complete (at most one group per buffer is outstanding at a time);
+    // phase_bits: the parity of each buffer's next phase.  A wait that
+    // succeeds consumes its phase; one that gives up leaves it pending.
+    uint32_t pend = 0;
+#define TSQR_WAIT_BUF(w, b, n)                                                                  \
+    do {                                                                                        \
+        const int b_ = (b);                                                                     \
+        w = tc::mbar_wait(tc::smem_u32(&S.mbar[b_]), (phase_bits >> b_) & 1u, (n));             \
+        if (w) {                                                                                \
+            phase_bits ^= 1u << b_;                                                             \
+            pend &= ~(1u << b_);                                                                \
+        }                                                                                       \
+    } while (0)
     if (nstage > 0) stage(0, 0);
     for (int s = 0; s < nstage && ok; ++s) {
         const int buf = s & 1;
@@ -195,13 +209,11 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
             tc::fence_after_sync();
             issue(s, buf);
         }
+        pend |= 1u << buf;
         if (s + 1 < nstage) {
             // buffer buf^1 was read by the MMAs of stage s-1: wait for them
             bool waited = true;
-            if (s >= 1) {
-                waited = tc::mbar_wait(tc::smem_u32(&S.mbar[buf ^ 1]), (phase_bits >> (buf ^ 1)) & 1u);
-                phase_bits ^= 1u << (buf ^ 1);
-            }
+            if (s >= 1) TSQR_WAIT_BUF(waited, buf ^ 1, tries);
             if (__syncthreads_or(!waited)) {
                 ok = false;
                 break;
@@ -211,19 +223,19 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
     }
     // wait for the last two stages' MMAs (in order of commit)
     if (ok && nstage > 0) {
-        bool waited = true;
-        if (nstage >= 2) {
-            const int b = (nstage - 2) & 1;
-            waited = tc::mbar_wait(tc::smem_u32(&S.mbar[b]), (phase_bits >> b) & 1u);
-            phase_bits ^= 1u << b;
-        }
-        const int b = (nstage - 1) & 1;
-        waited = tc::mbar_wait(tc::smem_u32(&S.mbar[b]), (phase_bits >> b) & 1u) && waited;
-        phase_bits ^= 1u << b;
-        if (__syncthreads_or(!waited)) ok = false;
+        bool w0 = true, w1;
+        if (nstage >= 2) TSQR_WAIT_BUF(w0, (nstage - 2) & 1, tries);
+        TSQR_WAIT_BUF(w1, (nstage - 1) & 1, tries);
+        if (__syncthreads_or(!(w0 && w1))) ok = false;
     }
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
+        // MMAs still in flight write TMEM: give them a full bounded wait to
+        // retire before it is freed
+        bool w;
+        if (pend & 1u) TSQR_WAIT_BUF(w, 0, tc::kMbarTries);
+        if (pend & 2u) TSQR_WAIT_BUF(w, 1, tc::kMbarTries);
+        (void)w;
     } else {
         tc::fence_after_sync();
         const int m = m0 + 32 * warp + (tid & 31);
@@ -258,6 +270,7 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
             }
         }
     }
+#undef TSQR_WAIT_BUF
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -272,7 +285,8 @@ void launch_gemm(dim3 grid, int M, int N, int64_t K, const float* A, int64_t lda
     attr.run([] {
         cudaFuncSetAttribute(tc_gemm_kernel<TRANS_A, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
-    tc_gemm_kernel<TRANS_A, NB><<<grid, 128, smem, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err);
+    tc_gemm_kernel<TRANS_A, NB><<<grid, 128, smem, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err,
+                                                         wait_tries().load(std::memory_order_relaxed));
 }
 
 int nb_for(int N) { return N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256)); }

@@ -621,6 +621,15 @@ void* cached_workspace(size_t bytes, tsqr_status* st) {
         return nullptr;
     }
     std::lock_guard<std::mutex> lk(mu);
+    if (buf[dev]) {
+        // a cudaDeviceReset since the allocation invalidates it: allocate again
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, buf[dev]) != cudaSuccess || at.type != cudaMemoryTypeDevice) {
+            (void)cudaGetLastError();
+            buf[dev] = nullptr;
+            cap[dev] = 0;
+        }
+    }
     if (cap[dev] < bytes) {
         if (buf[dev]) {
             cudaDeviceSynchronize();

@@ -333,215 +333,6 @@ __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
 }
 
 // ---------------------------------------------------------------------------
-// Warp tiles (FP32, n <= 32).  One warp factors a tile of 32*RPT rows by
-// itself: row lane + 32*i sits in register row y[i].  Every reduction is a
-// warp shuffle or a per-warp shared-memory transpose, so there is no block
-// barrier on the column chain, and the warps of a CTA (and of an SM) work on
-// independent tiles: the per-column latency (norm -> reflector -> dots ->
-// update) is hidden by the other tiles in flight instead of being paid once
-// per 512-row tile under block barriers.  Same arithmetic and output format
-// as factor_tile (V in place, T in the top block's upper triangle, R to the
-// next level), only the tile is shorter, so the tree has more levels.
-template <int NMAX>
-struct WarpFactorSmem {
-    __align__(16) float xpose[32 * xpose_stride<NMAX>()];  // transpose scratch of the dot products
-    __align__(16) float coef[NMAX];                         // update coefficients (0 off the trailing columns)
-    SCols<float, NMAX> Sc;                                  // V^T V (strict upper part, by column)
-    float tau[NMAX];
-    float rdiag[NMAX];
-};
-
-template <int NMAX, int RPT, int U = 4>
-__device__ __forceinline__ void factor_warp_tile(WarpFactorSmem<NMAX>& S, float* tile, int64_t ld, int ht, int n,
-                                                 float* Rt, int64_t ldr) {
-    constexpr int SP = xpose_stride<NMAX>();
-    static_assert(NMAX <= 32 && NMAX % U == 0, "warp tiles hold at most 32 columns");
-    const int lane = threadIdx.x & 31;
-    const int G = (n + U - 1) / U;
-    const int shift = (U * G) % NMAX;
-    // Register layout and rotation as in factor_tile: at group g position
-    // c < n - U*g holds column U*g + c, position NMAX - U*g + k holds v_k.
-    float y[RPT][NMAX];
-#pragma unroll
-    for (int i = 0; i < RPT; ++i) {
-        const int r = lane + 32 * i;
-#pragma unroll
-        for (int c = 0; c < NMAX; ++c) y[i][c] = (r < ht && c < n) ? tile[r + c * ld] : 0.f;
-    }
-    float* mine = S.xpose + lane * SP;
-
-    // Look-ahead: the norm of column j+1 is reduced (shuffles, square root,
-    // reciprocals) while the rest of step j's update is still being issued,
-    // so the next column's reflector is ready when the update ends.  Every
-    // group runs all U steps without a branch; steps past column n-1 work on
-    // zero columns (tau = 0, coefficient 0) and change nothing that is kept.
-    float sig2, alpha;
-    {
-        float s = 0.f;
-#pragma unroll
-        for (int i = 0; i < RPT; ++i)
-            if (i > 0 || lane > 0) s = fmaf(y[i][0], y[i][0], s);
-        alpha = __shfl_sync(kFull, y[0][0], 0);
-        sig2 = warp_sum(s);
-    }
-
-#pragma unroll 1
-    for (int g = 0; g < G; ++g) {
-        const int base = U * g;
-        const int live = n - base;
-        const int past0 = NMAX - base;
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int j = base + u;
-            // (a) reflector of column j from sigma^2 = ||x(j+1:, j)||^2 and
-            // alpha = x(j, j).  The xor butterfly leaves the bitwise same sum
-            // in every lane, so beta, tau and the scale agree across the warp.
-            const bool zero = (sig2 == 0.f);
-            const float nrm = sqrtf(fmaf(alpha, alpha, sig2));
-            const float beta = zero ? alpha : ((alpha >= 0.f) ? -nrm : nrm);
-            const float tau = zero ? 0.f : (beta - alpha) * recip(beta);
-            const float scale = zero ? 0.f : recip(alpha - beta);
-            // (b) v_j (v_j(j) = 1, 0 above the diagonal)
-#pragma unroll
-            for (int i = 0; i < RPT; ++i)
-                if (i > 0 || lane > j) y[i][u] *= scale;
-            const float v0 = (lane > j) ? y[0][u] : ((lane == j) ? 1.f : 0.f);
-            // (c) partial dots v_j . y[c] of every other position, four at a
-            // time into this lane's transpose row
-#pragma unroll
-            for (int c4 = 0; c4 < NMAX; c4 += 4) {
-                float q[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int c = c4 + e;
-                    q[e] = (c != u) ? v0 * y[0][c] : 0.f;
-#pragma unroll
-                    for (int i = 1; i < RPT; ++i)
-                        if (c != u) q[e] = fmaf(y[i][u], y[i][c], q[e]);
-                }
-                *reinterpret_cast<float4*>(mine + c4) = make_float4(q[0], q[1], q[2], q[3]);
-            }
-            __syncwarp();
-            // (d) lane c sums position c over the warp (pairwise, in four
-            // groups of eight rows), then publishes the update coefficient
-            // and, for finished reflectors, column j of V^T V
-            if (lane < NMAX) {
-                float part[4];
-#pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    float a[8];
-#pragma unroll
-                    for (int r = 0; r < 8; ++r) a[r] = S.xpose[(8 * h + r) * SP + lane];
-#pragma unroll
-                    for (int w = 4; w >= 1; w >>= 1)
-#pragma unroll
-                        for (int r = 0; r < w; ++r) a[r] += a[r + w];
-                    part[h] = a[0];
-                }
-                const float d = (part[0] + part[1]) + (part[2] + part[3]);
-                S.coef[lane] = (lane > u && lane < live) ? d : 0.f;
-                const int k = (lane >= past0) ? lane - past0 : ((lane < u) ? base + lane : -1);
-                if (k >= 0) S.Sc.c[j][k] = d;
-            }
-            if (lane == 0) {
-                S.tau[j] = tau;
-                S.rdiag[j] = beta;
-            }
-            __syncwarp();
-            // (e) x_c -= tau (v^T x_c) v on the positions after u: position
-            // u+1 first, then its norm is started, then the rest
-            float tv[RPT];
-            tv[0] = tau * v0;
-#pragma unroll
-            for (int i = 1; i < RPT; ++i) tv[i] = tau * y[i][u];
-            float cf[NMAX];
-#pragma unroll
-            for (int c4 = 0; c4 < NMAX; c4 += 4) {
-                if (c4 + 3 <= u) continue;
-                const float4 w4 = *reinterpret_cast<const float4*>(S.coef + c4);
-                cf[c4] = w4.x;
-                cf[c4 + 1] = w4.y;
-                cf[c4 + 2] = w4.z;
-                cf[c4 + 3] = w4.w;
-            }
-            if (u + 1 < NMAX) {
-                const int c = (u + 1 < NMAX) ? u + 1 : 0;  // keeps the index in range when u + 1 == NMAX
-#pragma unroll
-                for (int i = 0; i < RPT; ++i) y[i][c] = fmaf(-tv[i], cf[c], y[i][c]);
-                float s = 0.f;
-#pragma unroll
-                for (int i = 0; i < RPT; ++i)
-                    if (i > 0 || lane > j + 1) s = fmaf(y[i][c], y[i][c], s);
-                alpha = __shfl_sync(kFull, y[0][c], (j + 1) & 31);
-                sig2 = warp_sum(s);
-            }
-#pragma unroll
-            for (int c = u + 2; c < NMAX; ++c)
-#pragma unroll
-                for (int i = 0; i < RPT; ++i) y[i][c] = fmaf(-tv[i], cf[c], y[i][c]);
-        }
-#pragma unroll
-        for (int i = 0; i < RPT; ++i) {
-            float keep[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) keep[u] = y[i][u];
-#pragma unroll
-            for (int c = 0; c < NMAX - U; ++c) y[i][c] = y[i][c + U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) y[i][NMAX - U + u] = keep[u];
-        }
-    }
-    __syncwarp();  // tau, rdiag and V^T V of the last column are visible
-
-    // R (row r < n is lane r's slot 0) and V below the diagonal.
-    if (lane < n) {
-#pragma unroll
-        for (int c = 0; c < NMAX; ++c) {
-            const int k = (c + shift) % NMAX;
-            if (k < n) {
-                float v = (k > lane) ? y[0][c] : ((k == lane) ? S.rdiag[lane] : 0.f);
-                if (lane >= ht) v = 0.f;
-                Rt[lane + k * ldr] = v;
-            }
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < RPT; ++i) {
-        const int r = lane + 32 * i;
-        if (r < ht) {
-#pragma unroll
-            for (int c = 0; c < NMAX; ++c) {
-                const int k = (c + shift) % NMAX;
-                if (k < n && r > k) tile[r + k * ld] = y[i][c];
-            }
-        }
-    }
-    // T in the top block's upper triangle (diagonal included), row i by lane
-    // i: T(i,i) = tau_i, T(i,j) = -tau_j sum_{k=i}^{j-1} T(i,k) S(k,j).
-    if (lane < n && lane < ht) {
-        const int i = lane;
-        float trow[NMAX];
-        t_factor_row<float, NMAX>(S.Sc, S.tau, i, n, trow);
-#pragma unroll
-        for (int j = 0; j < NMAX; ++j)
-            if (j >= i && j < n) tile[i + j * ld] = trow[j];
-    }
-    __syncwarp();  // the next tile of this warp reuses S
-}
-
-template <int NMAX, int RPT, int WPB, int MINB, int U = 4>
-__global__ void __launch_bounds__(32 * WPB, MINB) factor_warp_tiles(FactorParams<float> p) {
-    constexpr int B = 32 * RPT;
-    __shared__ WarpFactorSmem<NMAX> S[WPB];
-    const int warp = threadIdx.x >> 5;
-    for (int64_t t = (int64_t)blockIdx.x * WPB + warp; t < p.ntiles; t += (int64_t)gridDim.x * WPB) {
-        const int64_t row0 = t * B;
-        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
-        factor_warp_tile<NMAX, RPT, U>(S[warp], p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n, p.ldr);
-    }
-}
-
-// ---------------------------------------------------------------------------
 // Column-split tiles (n <= NMAX <= 64, tiles of 32*RPT rows, FP32 or FP64).
 // The W = NMAX/CW warps of a CTA share one tile: warp w holds columns
 // [w*CW, w*CW + CW) of all 32*RPT rows (row lane + 32*i in y[i]), so a
