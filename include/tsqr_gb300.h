@@ -60,12 +60,21 @@ typedef enum tsqr_qr_algorithm {
 } tsqr_qr_algorithm;
 
 typedef struct tsqr_opts {
-    int precision;   /* tsqr_precision; ignored (always PLAIN) for FP64     */
-    int reorth;      /* qr only: 1 = second Gram-Schmidt projection (CGS2)  */
-    int panel;       /* qr only: panel width at which recursion stops, 0 = 32
-                        (the reference's N_B, block_QR.h:5)                 */
-    int algorithm;   /* qr only: tsqr_qr_algorithm, 0 = the reference's     */
-    int reserved[4]; /* must be zero                                        */
+    int precision;    /* tsqr_precision; ignored (always PLAIN) for FP64    */
+    int reorth;       /* 1 = one reorthogonalisation pass.  qr: a second
+                         Gram-Schmidt projection (CGS2).  tsqr_*_ex: a second
+                         TSQR of the computed Q in the same form, Q <- Q2 and
+                         R <- R2 R1 (the workspace grows by n x n elements) */
+    int panel;        /* qr only: panel width at which recursion stops, 0 = 32
+                         (the reference's N_B, block_QR.h:5)                */
+    int algorithm;    /* qr only: tsqr_qr_algorithm, 0 = the reference's    */
+    int fp64_scalars; /* tsqr_s_ex with TF32X3 only: 1 = each column's
+                         Householder norm, beta and tau computed in FP64
+                         (the tile stays FP32)                              */
+    int fp64_root;    /* tsqr_s_ex with TF32X3 only, n <= 32: 1 = the root of
+                         the reduction tree (at most one tile of stacked R
+                         factors) factored in FP64                          */
+    int reserved[2];  /* must be zero                                       */
 } tsqr_opts;
 
 /* Workspace bytes an ex call needs for an m x n problem of element size

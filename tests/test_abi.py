@@ -199,3 +199,32 @@ def test_noalloc_rejects_bad_arguments_before_any_cuda_call(tg):
     assert fn(1000, 32, fake, 1000, fake, 31, None) == 1   # ldr < n
     assert fn(16, 32, fake, 16, fake, 32, None) == 1       # m < n
     assert fn(0, 32, fake, 1, fake, 32, None) == 1         # empty
+
+
+def test_precision_form_options_and_reorth_sizes_need_no_gpu(tg):
+    """fp64_scalars / fp64_root belong to the TF32X3 form of tsqr_*_ex
+    (fp64_root for n <= 32); reorth adds an n x n factor to the workspace;
+    option values other than 0 and 1 are invalid; the host, implicit-Q and
+    blocked-QR entry points refuse the TSQR-only options before any CUDA
+    call."""
+    L = tg.lib()
+    fake = ctypes.c_void_p(0x1000)
+    o = tg._opts("plain")
+    base = L.tsqr_workspace_bytes(1 << 20, 32, 4, ctypes.byref(o))
+    o = tg._opts("plain", reorth=True)
+    assert L.tsqr_workspace_bytes(1 << 20, 32, 4, ctypes.byref(o)) >= base + 32 * 32 * 4
+    assert L.tsqr_workspace_bytes(1 << 20, 32, 4, ctypes.byref(tg._opts("plain", fp64_scalars=True))) == 0
+    assert L.tsqr_workspace_bytes(1 << 20, 32, 4, ctypes.byref(tg._opts("tf32x3", fp64_scalars=True))) > 0
+    assert L.tsqr_workspace_bytes(1 << 20, 32, 4, ctypes.byref(tg._opts("tf32x3", fp64_root=True))) > 0
+    assert L.tsqr_workspace_bytes(1 << 20, 48, 4, ctypes.byref(tg._opts("tf32x3", fp64_root=True))) == 0
+    bad = tg._opts("tf32x3")
+    bad.fp64_scalars = 2
+    assert L.tsqr_s_ex(1000, 32, fake, 1000, fake, 32, fake, 1 << 20, ctypes.byref(bad), None) == 1
+    o = tg._opts("plain", fp64_root=True)
+    assert L.tsqr_s_ex(1000, 32, fake, 1000, fake, 32, fake, 1 << 20, ctypes.byref(o), None) == 2
+    o = tg._opts("plain", reorth=True)
+    assert L.tsqr_s_ex(1 << 20, 32, fake, 1 << 20, fake, 32, fake, base, ctypes.byref(o), None) == 3
+    assert L.tsqr_s_host(1000, 32, fake, 1000, fake, 1000, fake, 32, fake, 1 << 20, ctypes.byref(o), None) == 2
+    assert L.tsqr_s_factor(1000, 32, fake, 1000, fake, 32, fake, 1 << 20, ctypes.byref(o), None) == 2
+    o = tg._opts("tf32x3", fp64_scalars=True)
+    assert L.qr_s_ex(1000, 64, fake, 1000, fake, 64, fake, 1 << 20, ctypes.byref(o), None) == 2

@@ -20,12 +20,20 @@ BUILD = os.path.join(ROOT, "tsqr_gb300", "_build")
 KNOWN = {
     # FP64 tile factor: 3 CTAs per SM cap it at 85 registers; the FP64 pipe
     # bounds this kernel
-    "tsqr::factor_split_tiles<double, 32, 4, 8, 3>": (788, 1312),
+    "tsqr::factor_split_tiles<double, 32, 4, 8, 3, false>": (788, 1312),
     # the 64-column tile holds 128 values per thread
-    "tsqr::factor_split_tiles<float, 64, 8, 16, 1>": (92, 92),
-    "tsqr::factor_split_tiles<float, 64, 8, 8, 1>": (44, 44),
-    "tsqr::factor_split_tiles<float, 64, 8, 4, 1>": (4, 4),
-    "tsqr::factor_split_tiles<float, 64, 8, 2, 1>": (4, 4),
+    "tsqr::factor_split_tiles<float, 64, 8, 16, 1, false>": (92, 92),
+    "tsqr::factor_split_tiles<float, 64, 8, 8, 1, false>": (44, 44),
+    "tsqr::factor_split_tiles<float, 64, 8, 4, 1, false>": (4, 4),
+    "tsqr::factor_split_tiles<float, 64, 8, 2, 1, false>": (4, 4),
+    # the precision form's fp64_scalars option: FP64 norm, beta and tau take
+    # register pairs on the owner's chain (an option, off by default)
+    "tsqr::factor_split_tiles<float, 16, 4, 16, 4, true>": (112, 248),
+    "tsqr::factor_split_tiles<float, 32, 4, 16, 2, true>": (112, 248),
+    "tsqr::factor_split_tiles<float, 64, 8, 16, 1, true>": (160, 160),
+    "tsqr::factor_split_tiles<float, 64, 8, 8, 1, true>": (68, 68),
+    "tsqr::factor_split_tiles<float, 64, 8, 4, 1, true>": (4, 4),
+    "tsqr::factor_split_tiles<float, 64, 8, 2, 1, true>": (4, 4),
     # batched kernels: per-problem descriptors cost registers
     "tsqr::batched_apply<64, 256, 2, 1>": (88, 128),
     "tsqr::batched_apply<32, 256, 2, 2>": (80, 112),
@@ -85,8 +93,8 @@ def test_no_new_or_larger_spills(spills):
     assert not bad, bad
 
 
-@pytest.mark.parametrize("kernel", ["tsqr::factor_split_tiles<float, 32, 4, 16, 2>",
-                                    "tsqr::factor_split_tiles<float, 16, 4, 16, 4>",
+@pytest.mark.parametrize("kernel", ["tsqr::factor_split_tiles<float, 32, 4, 16, 2, false>",
+                                    "tsqr::factor_split_tiles<float, 16, 4, 16, 4, false>",
                                     "tsqr::apply_tiles<float, 32, 256, 2, 2>",
                                     "tsqr::tc_apply_tiles<32, 512>"])
 def test_headline_kernels_do_not_spill(spills, kernel):

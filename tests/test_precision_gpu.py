@@ -199,3 +199,64 @@ def test_a_tensor_core_wait_that_runs_out_is_reported_and_the_next_call_succeeds
     for M0, dQ, dRr in ((A, dA, dR), (B, dB, dR2)):
         met = orc.metrics(M0, to_host(dQ), to_host(dRr))
         assert met["backward"] <= 1e-5 and met["orth"] <= 1e-5, met
+
+
+@pytest.mark.parametrize("m,n", [(27648, 32), (100000, 64), (70001, 13), (1000, 7), (300000, 16)])
+def test_fp64_scalars_option(orc, cuda, tg, m, n):
+    """tsqr_opts.fp64_scalars: each column's Householder norm, beta and tau in
+    FP64 inside the FP32 tile factorisation.  Same bar as the form; R agrees
+    with the default form's to the form's precision."""
+    A = orc.fill_uniform(m, n, np.float32, seed=31)
+    dA = to_dev(tg, A)
+    dR = tg.tsqr_(dA, precision="tf32x3", fp64_scalars=True)
+    dA0 = to_dev(tg, A)
+    dR0 = tg.tsqr_(dA0, precision="tf32x3")
+    Q, R = to_host(dA), to_host(dR)
+    met = orc.metrics(A, Q, R)
+    assert met["backward"] <= 1e-5 and met["orth"] <= 1e-5, met
+    R0 = to_host(dR0)
+    assert np.abs(R - R0).max() <= 1e-5 * np.abs(R0).max()
+
+
+@pytest.mark.parametrize("m,n", [(300000, 32), (27648, 32), (500, 20), (70001, 13)])
+def test_fp64_root_option(orc, cuda, tg, m, n):
+    """tsqr_opts.fp64_root: the root of the tree factored by the FP64 tree
+    (a single-tile problem: the whole of A).  Same bar as the form."""
+    A = orc.fill_uniform(m, n, np.float32, seed=32)
+    dA = to_dev(tg, A)
+    dR = tg.tsqr_(dA, precision="tf32x3", fp64_root=True)
+    met = orc.metrics(A, to_host(dA), to_host(dR))
+    assert met["backward"] <= 1e-5 and met["orth"] <= 1e-5, met
+    with pytest.raises(tg.TsqrError):
+        tg.tsqr_(to_dev(tg, orc.fill_uniform(1000, 48, np.float32, seed=1)), precision="tf32x3", fp64_root=True)
+
+
+@pytest.mark.parametrize("form,dtype,m,n", [("plain", np.float32, 27648, 32), ("plain", np.float32, 70001, 13),
+                                            ("plain", np.float64, 27648, 32), ("tf32x3", np.float32, 100000, 32),
+                                            ("tf32x3", np.float32, 300, 20)])
+def test_tsqr_reorthogonalisation_pass(orc, cuda, tg, form, dtype, m, n):
+    """tsqr_opts.reorth for TSQR: a second TSQR of the computed Q, R <- R2 R1.
+    The result meets the form's bar (plain: 10 n u; tf32x3: 1e-5), and R
+    agrees with the single pass's R (R2 is the identity to rounding)."""
+    import torch
+    A = orc.fill_uniform(m, n, dtype, seed=33)
+    tdt = torch.float32 if dtype == np.float32 else torch.float64
+    dA = tg.empty_colmajor(m, n, tdt, "cuda")
+    dA.copy_(torch.from_numpy(np.ascontiguousarray(A)))
+    w = torch.zeros(tg.workspace_bytes(m, n, tdt, precision=form, reorth=True), dtype=torch.uint8, device="cuda")
+    assert w.numel() > tg.workspace_bytes(m, n, tdt, precision=form)
+    dR = tg.tsqr_(dA, precision=form, reorth=True, work=w)
+    torch.cuda.synchronize()
+    Q, R = to_host(dA), to_host(dR)
+    met = orc.metrics(A, Q, R)
+    u = orc.unit_roundoff(dtype)
+    bar = 1e-5 if form == "tf32x3" else 10 * n * u
+    assert met["backward"] <= bar and met["orth"] <= bar, met
+    assert np.all(np.tril(R, -1) == 0)
+    dA1 = tg.empty_colmajor(m, n, tdt, "cuda")
+    dA1.copy_(torch.from_numpy(np.ascontiguousarray(A)))
+    R1 = to_host(tg.tsqr_(dA1, precision=form))
+    tol = 1e-5 if form == "tf32x3" else 100 * n * u
+    assert np.abs(R - R1).max() <= tol * np.abs(R1).max()
+    if form == "tf32x3":
+        assert tg.lib().tsqr_workspace_check(w.data_ptr()) == 0

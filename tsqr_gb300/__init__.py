@@ -41,7 +41,8 @@ class TsqrError(RuntimeError):
 
 class Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("reorth", ctypes.c_int), ("panel", ctypes.c_int),
-                ("algorithm", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+                ("algorithm", ctypes.c_int), ("fp64_scalars", ctypes.c_int), ("fp64_root", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class CheckResult(ctypes.Structure):
@@ -136,12 +137,14 @@ def _check(st, where):
 _ALGO = {"block_gs": 0, "householder": 1, 0: 0, 1: 1}
 
 
-def _opts(precision="plain", reorth=False, panel=0, algorithm="block_gs"):
+def _opts(precision="plain", reorth=False, panel=0, algorithm="block_gs", fp64_scalars=False, fp64_root=False):
     o = Opts()
     o.precision = _PREC[precision]
     o.reorth = 1 if reorth else 0
     o.panel = int(panel)
     o.algorithm = _ALGO[algorithm]
+    o.fp64_scalars = 1 if fp64_scalars else 0
+    o.fp64_root = 1 if fp64_root else 0
     return o
 
 
@@ -154,8 +157,8 @@ def _elem(dtype):
     raise TsqrError(1, "dtype %s" % (dtype,))
 
 
-def workspace_bytes(m, n, dtype, precision="plain"):
-    o = _opts(precision)
+def workspace_bytes(m, n, dtype, precision="plain", reorth=False, fp64_scalars=False, fp64_root=False):
+    o = _opts(precision, reorth, fp64_scalars=fp64_scalars, fp64_root=fp64_root)
     return int(lib().tsqr_workspace_bytes(m, n, _elem(dtype), ctypes.byref(o)))
 
 
@@ -302,17 +305,19 @@ def check_(A, Q, R, atol=1e-4, rtol=1e-5, work=None, stream=None):
     return out
 
 
-def tsqr_(A, R=None, precision="plain", work=None, stream=None):
+def tsqr_(A, R=None, precision="plain", work=None, stream=None, reorth=False, fp64_scalars=False, fp64_root=False):
     """Factor the column-major m x n CUDA tensor A in place: A <- Q.
-    Returns R (n x n, column-major).  precision: "plain", "tf32x3",
-    "bf16x3" (the last two for float32 only)."""
+    Returns R (n x n, column-major).  precision: "plain" or "tf32x3" (float32
+    only).  reorth: one reorthogonalisation pass (a second TSQR of Q).
+    fp64_scalars / fp64_root: options of the "tf32x3" form (FP64 Householder
+    norm, beta and tau; FP64 root combine, n <= 32)."""
     import torch
     m, n = A.shape
     lda = _ld(A)
     if R is None:
         R = empty_colmajor(n, n, A.dtype, A.device)
     ldr = _ld(R)
-    o = _opts(precision)
+    o = _opts(precision, reorth, fp64_scalars=fp64_scalars, fp64_root=fp64_root)
     nbytes = int(lib().tsqr_workspace_bytes(m, n, A.element_size(), ctypes.byref(o)))
     if nbytes == 0:
         raise TsqrError(2, "tsqr_ workspace (m=%d n=%d)" % (m, n))

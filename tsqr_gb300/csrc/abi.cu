@@ -27,12 +27,33 @@ tsqr_status check_common(int64_t m, int64_t n, const T* A, int64_t lda, const T*
     if (m < 1 || n < 1 || m < n) return TSQR_ERR_INVALID_ARG;
     if (lda < m || ldr < n) return TSQR_ERR_INVALID_ARG;
     if (A == nullptr || R == nullptr) return TSQR_ERR_INVALID_ARG;
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 2; ++i)
         if (o.reserved[i] != 0) return TSQR_ERR_INVALID_ARG;
+    if (o.fp64_scalars < 0 || o.fp64_scalars > 1 || o.fp64_root < 0 || o.fp64_root > 1) return TSQR_ERR_INVALID_ARG;
     if (o.algorithm != TSQR_QR_BLOCK_GS && o.algorithm != TSQR_QR_HOUSEHOLDER) return TSQR_ERR_INVALID_ARG;
     if (o.precision < TSQR_PRECISION_PLAIN || o.precision > TSQR_PRECISION_BF16X3) return TSQR_ERR_INVALID_ARG;
     if (o.panel < 0 || o.reorth < 0 || o.reorth > 1) return TSQR_ERR_INVALID_ARG;
     return TSQR_OK;
+}
+
+constexpr size_t kAlignAbi = 256;
+size_t align_up(size_t b) { return (b + kAlignAbi - 1) / kAlignAbi * kAlignAbi; }
+
+// Workspace of tsqr_*_ex: the form's tree workspace, then (reorth) the
+// second pass's n x n R.  0 for what the library does not cover.
+template <typename T>
+size_t tsqr_ex_workspace(int64_t m, int64_t n, const tsqr_opts& o) {
+    const bool prec = sizeof(T) == 4 && o.precision == TSQR_PRECISION_TF32X3;
+    if (n > max_tsqr_n<T>()) return 0;
+    if (sizeof(T) == 4 && o.precision == TSQR_PRECISION_BF16X3) return 0;
+    if (!prec && (o.fp64_scalars || o.fp64_root)) return 0;
+    if (prec && o.fp64_root && n > 32) return 0;
+    tsqr::PrecFlags f;
+    f.norm64 = o.fp64_scalars != 0;
+    f.root64 = o.fp64_root != 0;
+    const size_t base = prec ? tsqr::tsqr_precision_workspace(m, n, f) : tsqr::tsqr_plain_workspace<T>(m, n);
+    if (base == 0) return 0;
+    return o.reorth ? align_up(base) + align_up((size_t)(n * n) * sizeof(T)) : base;
 }
 
 template <typename T>
@@ -41,13 +62,34 @@ tsqr_status tsqr_ex(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, 
     const tsqr_opts o = opts_or_default(op);
     tsqr_status st = check_common<T>(m, n, A, lda, R, ldr, o);
     if (st != TSQR_OK) return st;
-    if (n > max_tsqr_n<T>()) return TSQR_ERR_UNSUPPORTED;
-    if (sizeof(T) == 8 || o.precision == TSQR_PRECISION_PLAIN)
-        return tsqr::tsqr_plain<T>(m, n, A, lda, R, ldr, work, work_bytes, (cudaStream_t)stream);
-    if (o.precision == TSQR_PRECISION_TF32X3)
-        return tsqr::tsqr_precision(m, n, reinterpret_cast<float*>(A), lda, reinterpret_cast<float*>(R), ldr, work,
-                                    work_bytes, (cudaStream_t)stream);
-    return TSQR_ERR_UNSUPPORTED;
+    if (tsqr_ex_workspace<T>(m, n, o) == 0) return TSQR_ERR_UNSUPPORTED;
+    const cudaStream_t s = (cudaStream_t)stream;
+    const bool prec = sizeof(T) == 4 && o.precision == TSQR_PRECISION_TF32X3;
+    tsqr::PrecFlags f;
+    f.norm64 = o.fp64_scalars != 0;
+    f.root64 = o.fp64_root != 0;
+    // one TSQR pass of the chosen form over A, its R to Rp; a second pass
+    // keeps the first pass's tensor-core status
+    auto pass = [&](T* Rp, int64_t ldrp, size_t bytes, bool first) -> tsqr_status {
+        if (prec) {
+            f.clear_status = first;
+            return tsqr::tsqr_precision(m, n, reinterpret_cast<float*>(A), lda, reinterpret_cast<float*>(Rp), ldrp,
+                                        work, bytes, s, f);
+        }
+        return tsqr::tsqr_plain<T>(m, n, A, lda, Rp, ldrp, work, bytes, s);
+    };
+    if (!o.reorth) return pass(R, ldr, work_bytes, true);
+    // one reorthogonalisation pass: Q1 R1 = A, then Q2 R2 = Q1, so that
+    // A = Q2 (R2 R1)
+    const size_t need = tsqr_ex_workspace<T>(m, n, o);
+    if (work == nullptr || work_bytes < need) return TSQR_ERR_WORKSPACE;
+    const size_t base = need - align_up((size_t)(n * n) * sizeof(T));
+    T* R2 = reinterpret_cast<T*>(reinterpret_cast<char*>(work) + base);
+    st = pass(R, ldr, base, true);
+    if (st != TSQR_OK) return st;
+    st = pass(R2, n, base, false);
+    if (st != TSQR_OK) return st;
+    return tsqr::upper_product<T>((int)n, R2, n, R, ldr, s);
 }
 
 // Implicit-Q form: the up-sweep alone, and later the down-sweep alone, on
@@ -58,7 +100,8 @@ tsqr_status factor_ex(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr
     const tsqr_opts o = opts_or_default(op);
     tsqr_status st = check_common<T>(m, n, A, lda, R, ldr, o);
     if (st != TSQR_OK) return st;
-    if (n > max_tsqr_n<T>() || o.precision != TSQR_PRECISION_PLAIN) return TSQR_ERR_UNSUPPORTED;
+    if (n > max_tsqr_n<T>() || o.precision != TSQR_PRECISION_PLAIN || o.reorth || o.fp64_scalars || o.fp64_root)
+        return TSQR_ERR_UNSUPPORTED;
     return tsqr::tsqr_plain<T>(m, n, A, lda, R, ldr, work, work_bytes, (cudaStream_t)stream, tsqr::kPhaseUp);
 }
 
@@ -75,7 +118,7 @@ tsqr_status qr_ex(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, vo
     const tsqr_opts o = opts_or_default(op);
     tsqr_status st = check_common<T>(m, n, A, lda, R, ldr, o);
     if (st != TSQR_OK) return st;
-    if (o.panel > max_tsqr_n<T>()) return TSQR_ERR_UNSUPPORTED;
+    if (o.panel > max_tsqr_n<T>() || o.fp64_scalars || o.fp64_root) return TSQR_ERR_UNSUPPORTED;
     if (sizeof(T) == 4 && o.precision == TSQR_PRECISION_BF16X3) return TSQR_ERR_UNSUPPORTED;
     return tsqr::qr_run<T>(m, n, A, lda, R, ldr, work, work_bytes, o, (cudaStream_t)stream);
 }
@@ -108,7 +151,8 @@ tsqr_status tsqr_host_call(int64_t m, int64_t n, const T* A, int64_t lda, T* Q, 
     if (st != TSQR_OK) return st;
     if (Q == nullptr || ldq < m) return TSQR_ERR_INVALID_ARG;
     if (n > max_tsqr_n<T>()) return TSQR_ERR_UNSUPPORTED;
-    if (o.precision == TSQR_PRECISION_BF16X3 || (sizeof(T) == 8 && o.precision != TSQR_PRECISION_PLAIN))
+    if (o.precision == TSQR_PRECISION_BF16X3 || (sizeof(T) == 8 && o.precision != TSQR_PRECISION_PLAIN) || o.reorth ||
+        o.fp64_scalars || o.fp64_root)
         return TSQR_ERR_UNSUPPORTED;
     return tsqr::tsqr_host<T>(m, n, A, lda, Q, ldq, R, ldr, work, work_bytes,
                               o.precision == TSQR_PRECISION_TF32X3, (cudaStream_t)stream);
@@ -121,10 +165,8 @@ extern "C" {
 size_t tsqr_workspace_bytes(int64_t m, int64_t n, int elem_bytes, const tsqr_opts* opts) {
     const tsqr_opts o = opts_or_default(opts);
     if (m < 1 || n < 1 || m < n) return 0;
-    if (elem_bytes == 4 && o.precision == TSQR_PRECISION_TF32X3)
-        return n <= 64 ? tsqr::tsqr_precision_workspace(m, n) : 0;
-    if (elem_bytes == 4) return n <= 64 ? tsqr::tsqr_plain_workspace<float>(m, n) : 0;
-    if (elem_bytes == 8) return n <= 32 ? tsqr::tsqr_plain_workspace<double>(m, n) : 0;
+    if (elem_bytes == 4) return tsqr_ex_workspace<float>(m, n, o);
+    if (elem_bytes == 8) return tsqr_ex_workspace<double>(m, n, o);
     return 0;
 }
 
@@ -231,10 +273,10 @@ tsqr_status tsqr_batched_s(int count, float* const* A, const int64_t* m, const i
     if (count < 0) return TSQR_ERR_INVALID_ARG;
     if (count == 0) return TSQR_OK;
     if (!A || !m || !n || !lda || !R || !ldr) return TSQR_ERR_INVALID_ARG;
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 2; ++i)
         if (o.reserved[i] != 0) return TSQR_ERR_INVALID_ARG;
     if (o.algorithm != TSQR_QR_BLOCK_GS && o.algorithm != TSQR_QR_HOUSEHOLDER) return TSQR_ERR_INVALID_ARG;
-    if (o.precision != TSQR_PRECISION_PLAIN) return TSQR_ERR_UNSUPPORTED;
+    if (o.precision != TSQR_PRECISION_PLAIN || o.fp64_scalars || o.fp64_root) return TSQR_ERR_UNSUPPORTED;
     for (int i = 0; i < count; ++i) {
         if (m[i] < 1 || n[i] < 1 || m[i] < n[i] || lda[i] < m[i] || ldr[i] < n[i]) return TSQR_ERR_INVALID_ARG;
         if (A[i] == nullptr || R[i] == nullptr) return TSQR_ERR_INVALID_ARG;

@@ -123,14 +123,28 @@ template <typename T>
 tsqr_status qr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
                    const tsqr_opts& o, cudaStream_t s);
 
+// R <- R2 R of two n x n upper triangular factors (n <= 64 for float, 32
+// for double), zeros below the diagonal (tsqr.cu).
+template <typename T>
+tsqr_status upper_product(int n, const T* R2, int64_t ld2, T* R, int64_t ldr, cudaStream_t s);
+
 // Library-owned per-device buffer for the reference-signature entry points.
 void* cached_workspace(size_t bytes, tsqr_status* st);
 
 }  // namespace tsqr
 
 namespace tsqr {
-// Precision form of TSQR (tsqr.cu + tc_apply.cu), FP32 only.
-size_t tsqr_precision_workspace(int64_t m, int64_t n);
+// Precision form of TSQR (tsqr.cu + tc_apply.cu), FP32 only.  Options:
+// norm64 -- per-column norm, beta and tau in FP64 (tsqr_opts.fp64_scalars);
+// root64 -- root combine in FP64, n <= 32 (tsqr_opts.fp64_root);
+// clear_status -- zero the status word first (off for a second pass that
+// must keep the first pass's report).
+struct PrecFlags {
+    bool norm64 = false;
+    bool root64 = false;
+    bool clear_status = true;
+};
+size_t tsqr_precision_workspace(int64_t m, int64_t n, PrecFlags f = PrecFlags());
 // TSQR of host-resident A with host Q and R, transfers pipelined with the
 // level-0 kernels (tsqr.cu).  prec: the precision form (FP32 only).
 template <typename T>
@@ -139,7 +153,7 @@ template <typename T>
 tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int64_t ldq, T* hR, int64_t ldr,
                       void* work, size_t work_bytes, bool prec, cudaStream_t s);
 tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
-                           size_t work_bytes, cudaStream_t s);
+                           size_t work_bytes, cudaStream_t s, PrecFlags f = PrecFlags());
 }  // namespace tsqr
 
 namespace tsqr {

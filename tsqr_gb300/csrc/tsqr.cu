@@ -44,7 +44,7 @@ struct TileCfg {
 
 // Factor on column-split tiles (factor_split_tiles: NMAX/CW warps per
 // 32*RPT-row tile), with the same apply kernel as TileCfg.
-template <typename T, int NMAX, int CW, int RPT, int MINB, int ANT, int AMINB>
+template <typename T, int NMAX, int CW, int RPT, int MINB, int ANT, int AMINB, bool N64 = false>
 struct SplitCfg {
     static constexpr int kRows = 32 * RPT;
     static constexpr int ARPT = kRows / ANT;
@@ -56,12 +56,12 @@ struct SplitCfg {
         // kernel would spend 7/8 of them on zero rows.
         constexpr int W32 = 32 * (NMAX / CW);
         if constexpr (RPT > 2 && NMAX <= 64)
-            if (p.ntiles == 1 && p.h <= 64) return factor_split_tiles<T, NMAX, CW, 2, 1><<<1, W32, 0, s>>>(p);
+            if (p.ntiles == 1 && p.h <= 64) return factor_split_tiles<T, NMAX, CW, 2, 1, N64><<<1, W32, 0, s>>>(p);
         if constexpr (RPT > 4)
-            if (p.ntiles == 1 && p.h <= 128) return factor_split_tiles<T, NMAX, CW, 4, 1><<<1, W32, 0, s>>>(p);
+            if (p.ntiles == 1 && p.h <= 128) return factor_split_tiles<T, NMAX, CW, 4, 1, N64><<<1, W32, 0, s>>>(p);
         if constexpr (RPT > 8)
-            if (p.ntiles == 1 && p.h <= 256) return factor_split_tiles<T, NMAX, CW, 8, 1><<<1, W32, 0, s>>>(p);
-        factor_split_tiles<T, NMAX, CW, RPT, MINB><<<grid, W32, 0, s>>>(p);
+            if (p.ntiles == 1 && p.h <= 256) return factor_split_tiles<T, NMAX, CW, 8, 1, N64><<<1, W32, 0, s>>>(p);
+        factor_split_tiles<T, NMAX, CW, RPT, MINB, N64><<<grid, W32, 0, s>>>(p);
     }
     static void apply(const ApplyParams<T>& p, int grid, cudaStream_t s) {
         TileCfg<T, NMAX, ANT, ARPT, 1, AMINB>::apply(p, grid, s);
@@ -223,22 +223,23 @@ struct PrecCfg {
     KernelSet<float> ks;
 };
 
-PrecCfg pick_precision(int n) {
+// The tile factorisation is the plain FP32 kernel; with norm64
+// (tsqr_opts.fp64_scalars) its variant whose per-column norm, beta and tau
+// are computed in FP64.
+PrecCfg pick_precision(int n, bool norm64 = false) {
     PrecCfg c;
-    // The tile factorisation is the plain FP32 kernel.  Computing the
-    // per-column norm, beta and tau in FP64 (the NORM64 variant) was measured
-    // at 2.7x the FP32 factor time on GB300's FP64 pipe (4.66 ms vs 1.73 ms
-    // at 4,194,304 x 32) with no gain in the error figures, so the FP64 part
-    // of this form is the root combine only.
     if (n <= 16) {
         c.nmax = 16;
-        c.ks = make_set<SplitCfg<float, 16, 4, 16, 4, 256, 3>, float>();
+        c.ks = norm64 ? make_set<SplitCfg<float, 16, 4, 16, 4, 256, 3, true>, float>()
+                      : make_set<SplitCfg<float, 16, 4, 16, 4, 256, 3>, float>();
     } else if (n <= 32) {
         c.nmax = 32;
-        c.ks = make_set<SplitCfg<float, 32, 4, 16, 2, 256, 2>, float>();
+        c.ks = norm64 ? make_set<SplitCfg<float, 32, 4, 16, 2, 256, 2, true>, float>()
+                      : make_set<SplitCfg<float, 32, 4, 16, 2, 256, 2>, float>();
     } else if (n <= 64) {
         c.nmax = 64;
-        c.ks = make_set<SplitCfg<float, 64, 8, 16, 1, 256, 1>, float>();
+        c.ks = norm64 ? make_set<SplitCfg<float, 64, 8, 16, 1, 256, 1, true>, float>()
+                      : make_set<SplitCfg<float, 64, 8, 16, 1, 256, 1>, float>();
     }
     c.rows = c.ks.rows;
     return c;
@@ -248,15 +249,9 @@ struct PrecLayout {
     size_t status = 0, levels = 0, root = 0, rootws = 0, total = 0;
 };
 
-// Root combine in FP64 (the root level converted to double, factored by the
-// FP64 tree, converted back).  Off: on GB300 the FP64 factorisation of even
-// the 64 x 32 root of a 4,194,304 x 32 problem took 0.47 ms of a 2.25 ms
-// call (FP64 runs at a small fraction of the FP32 rate there), and the FP32
-// root already meets the form's error bar.  The path is kept, tested by the
-// same code as the FP64 entry points, for builds that turn it on.
-constexpr bool kRoot64 = false;
-
-PrecLayout prec_layout(int64_t m, int64_t n, const PrecCfg& c) {
+// Root combine in FP64 (tsqr_opts.fp64_root, n <= 32): the root level
+// converted to double, factored by the FP64 tree, converted back.
+PrecLayout prec_layout(int64_t m, int64_t n, const PrecCfg& c, bool root64_opt = false) {
     PrecLayout L;
     L.status = 0;
     L.levels = kAlign;
@@ -264,7 +259,7 @@ PrecLayout prec_layout(int64_t m, int64_t n, const PrecCfg& c) {
     const size_t lev = plan_levels<float>(m, n, nullptr, m, c.rows, nullptr, &lv);
     L.root = L.levels + lev;
     const int64_t hroot = lv.back().h;
-    const bool root64 = kRoot64 && n <= 32;
+    const bool root64 = root64_opt && n <= 32;
     const size_t rootbytes = root64 ? (size_t)round_up(hroot * n * 8 + n * n * 8, (int64_t)kAlign) : 0;
     L.rootws = L.root + rootbytes;
     L.total = L.rootws + (root64 ? round_up((int64_t)tsqr_plain_workspace<double>(hroot, n), (int64_t)kAlign) : 0);
@@ -275,25 +270,26 @@ PrecLayout prec_layout(int64_t m, int64_t n, const PrecCfg& c) {
 
 bool tc_apply_level(const ApplyParams<float>& p, int nmax, int rows, int* err, cudaStream_t s);
 
-size_t tsqr_precision_workspace(int64_t m, int64_t n) {
-    PrecCfg c = pick_precision((int)n);
+size_t tsqr_precision_workspace(int64_t m, int64_t n, PrecFlags f) {
+    PrecCfg c = pick_precision((int)n, f.norm64);
     if (!c.ks.factor) return 0;
-    return prec_layout(m, n, c).total;
+    return prec_layout(m, n, c, f.root64).total;
 }
 
 tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
-                           size_t work_bytes, cudaStream_t s) {
-    PrecCfg c = pick_precision((int)n);
+                           size_t work_bytes, cudaStream_t s, PrecFlags f) {
+    PrecCfg c = pick_precision((int)n, f.norm64);
     if (!c.ks.factor) return TSQR_ERR_UNSUPPORTED;
-    const PrecLayout PL = prec_layout(m, n, c);
+    if (f.root64 && n > 32) return TSQR_ERR_UNSUPPORTED;
+    const PrecLayout PL = prec_layout(m, n, c, f.root64);
     if (work == nullptr || work_bytes < PL.total) return TSQR_ERR_WORKSPACE;
     char* base = reinterpret_cast<char*>(work);
     int* err = reinterpret_cast<int*>(base + PL.status);
     std::vector<Level<float>> lv;
     plan_levels<float>(m, n, A, lda, c.rows, base + PL.levels, &lv);
     const int L = (int)lv.size();
-    if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
-    const bool root64 = kRoot64 && n <= 32;
+    if (f.clear_status && cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
+    const bool root64 = f.root64;
     const int top = root64 ? L - 1 : L;  // levels factored in FP32 below the root
     for (int l = 0; l < top; ++l) {
         FactorParams<float> fp;
@@ -605,6 +601,43 @@ template tsqr_status tsqr_host<float>(int64_t, int64_t, const float*, int64_t, f
                                       void*, size_t, bool, cudaStream_t);
 template tsqr_status tsqr_host<double>(int64_t, int64_t, const double*, int64_t, double*, int64_t, double*,
                                        int64_t, void*, size_t, bool, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// R <- R2 R (both upper triangular), for the reorthogonalisation pass of
+// tsqr_*_ex.  One CTA: both factors are read into shared memory first, so R
+// may be overwritten; thread (i, j) forms sum_{k=i}^{j} R2(i,k) R(k,j).
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T, int NMAX>
+__global__ void upper_product_kernel(int n, const T* __restrict__ R2, int64_t ld2, T* R, int64_t ldr) {
+    __shared__ T a[NMAX][NMAX + 1], b[NMAX][NMAX + 1];
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = e % n, j = e / n;
+        a[i][j] = R2[i + j * ld2];
+        b[i][j] = R[i + j * ldr];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = e % n, j = e / n;
+        T s = T(0);
+        for (int k = i; k <= j; ++k) s += a[i][k] * b[k][j];
+        R[i + j * ldr] = (i <= j) ? s : T(0);
+    }
+}
+
+}  // namespace
+
+template <typename T>
+tsqr_status upper_product(int n, const T* R2, int64_t ld2, T* R, int64_t ldr, cudaStream_t s) {
+    constexpr int NMAX = sizeof(T) == 4 ? 64 : 32;
+    if (n < 1 || n > NMAX) return TSQR_ERR_UNSUPPORTED;
+    upper_product_kernel<T, NMAX><<<1, 256, 0, s>>>(n, R2, ld2, R, ldr);
+    log_launch(kTagTc + 902, s);
+    return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
+}
+template tsqr_status upper_product<float>(int, const float*, int64_t, float*, int64_t, cudaStream_t);
+template tsqr_status upper_product<double>(int, const double*, int64_t, double*, int64_t, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Per-device workspace cache for the reference-signature entry points, whose

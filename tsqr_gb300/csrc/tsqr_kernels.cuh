@@ -498,9 +498,14 @@ __device__ __forceinline__ T warp_colsum(const T (&q)[CW], T* scratch, int lane)
 // VECV: publish the reflector in the 16-byte vector layout (VbufLayout).
 // Off for the 64-column tile and for the batched kernels, whose registers
 // leave no room for the aligned quads it needs (more spills with it).
-template <typename T, int NMAX, int CW, int RPT, bool VECV = (NMAX <= 32)>
+// N64: the owner's column norm (sigma^2, accumulated and reduced), alpha and
+// the reflector scalars beta, tau and 1/(alpha - beta) in FP64, rounded to
+// the tile's type once computed; the tile, the dot products and the updates
+// stay in T.  (The precision form's option fp64_scalars.)
+template <typename T, int NMAX, int CW, int RPT, bool VECV = (NMAX <= 32), bool N64 = false>
 __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, RPT>& S, T* tile, int64_t ld, int ht,
                                                   int n, T* Rt, int64_t ldr) {
+    using SC = typename std::conditional<N64, double, T>::type;  // type of the reflector scalars
     constexpr int W = NMAX / CW;
     constexpr int U = 4;
     constexpr int VN = Vec16<T>::N;
@@ -520,11 +525,11 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
     // NMAX <= 32; the 64-column tile, already at its register limit, runs
     // faster with the plain operations (level-0 factor at 4,194,304 x 64:
     // 3.25 against 3.78 ms).
-    auto rsq = [](T x) {
+    auto rsq = [](SC x) {
         if constexpr (NMAX <= 32) return refl_sqrt(x);
         else return sqrt_t(x);
     };
-    auto rcp = [](T x) {
+    auto rcp = [](SC x) {
         if constexpr (NMAX <= 32) return refl_recip(x);
         else return recip(x);
     };
@@ -556,13 +561,13 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
             // ---- owner: reflectors of columns pc0 .. pc0+nloc-1, in groups of
             // U with the register rotation of factor_tile, and the norm of the
             // next column reduced while the current update is issued
-            T sig2, alpha;
+            SC sig2, alpha;
             {
-                T s4[4] = {T(0), T(0), T(0), T(0)};
+                SC s4[4] = {SC(0), SC(0), SC(0), SC(0)};
 #pragma unroll
                 for (int i = 0; i < RPT; ++i)
-                    if (below(i, pc0)) s4[i & 3] = fmadd(y[i][0], y[i][0], s4[i & 3]);
-                alpha = __shfl_sync(kFull, diag_slot(y, 0, pc0), pc0 & 31);
+                    if (below(i, pc0)) s4[i & 3] = fmadd((SC)y[i][0], (SC)y[i][0], s4[i & 3]);
+                alpha = (SC)__shfl_sync(kFull, diag_slot(y, 0, pc0), pc0 & 31);
                 sig2 = warp_sum((s4[0] + s4[1]) + (s4[2] + s4[3]));
             }
 #pragma unroll 1
@@ -573,11 +578,12 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int j = pc0 + base + u;
-                    const bool zero = (sig2 == T(0));
-                    const T nrm = rsq(fmadd(alpha, alpha, sig2));
-                    const T beta = zero ? alpha : ((alpha >= T(0)) ? -nrm : nrm);
-                    const T tau = zero ? T(0) : (beta - alpha) * rcp(beta);
-                    const T scale = zero ? T(0) : rcp(alpha - beta);
+                    const bool zero = (sig2 == SC(0));
+                    const SC nrm = rsq(fmadd(alpha, alpha, sig2));
+                    const SC beta_s = zero ? alpha : ((alpha >= SC(0)) ? -nrm : nrm);
+                    const T beta = (T)beta_s;
+                    const T tau = zero ? T(0) : (T)((beta_s - alpha) * rcp(beta_s));
+                    const T scale = zero ? T(0) : (T)rcp(alpha - beta_s);
 #pragma unroll
                     for (int i = 0; i < RPT; ++i)
                         if (below(i, j)) y[i][u] *= scale;
@@ -619,11 +625,11 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
                         const int c = (u + 1 < CW) ? u + 1 : 0;  // keeps the index in range when u + 1 == CW
 #pragma unroll
                         for (int i = 0; i < RPT; ++i) y[i][c] = fmadd(-tv[i], cf[c], y[i][c]);
-                        T s4[4] = {T(0), T(0), T(0), T(0)};  // four chains instead of one RPT-deep one
+                        SC s4[4] = {SC(0), SC(0), SC(0), SC(0)};  // four chains instead of one RPT-deep one
 #pragma unroll
                         for (int i = 0; i < RPT; ++i)
-                            if (below(i, j + 1)) s4[i & 3] = fmadd(y[i][c], y[i][c], s4[i & 3]);
-                        alpha = __shfl_sync(kFull, diag_slot(y, c, j + 1), (j + 1) & 31);
+                            if (below(i, j + 1)) s4[i & 3] = fmadd((SC)y[i][c], (SC)y[i][c], s4[i & 3]);
+                        alpha = (SC)__shfl_sync(kFull, diag_slot(y, c, j + 1), (j + 1) & 31);
                         sig2 = warp_sum((s4[0] + s4[1]) + (s4[2] + s4[3]));
                     }
 #pragma unroll
@@ -725,14 +731,14 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
     step_barrier(W * 32);  // S is reused by the CTA's next tile
 }
 
-template <typename T, int NMAX, int CW, int RPT, int MINB>
+template <typename T, int NMAX, int CW, int RPT, int MINB, bool N64 = false>
 __global__ void __launch_bounds__(32 * (NMAX / CW), MINB) factor_split_tiles(FactorParams<T> p) {
     constexpr int B = 32 * RPT;
     __shared__ SplitFactorSmem<T, NMAX, CW, RPT> S;
     for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
         const int64_t row0 = t * B;
         const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
-        factor_split_tile<T, NMAX, CW, RPT>(S, p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n, p.ldr);
+        factor_split_tile<T, NMAX, CW, RPT, (NMAX <= 32), N64>(S, p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n, p.ldr);
     }
 }
 
