@@ -5,9 +5,9 @@
                     [--workload tsqr|batch|qr] [--dtype f32|f64] [--reorth] [--algorithm block_gs|householder]
 
 One step = one TSQR (A <- Q, R) of the whole matrix through libtsqr_gb300's C
-ABI.  Input: A = U diag(sigma) V^T with U, V orthonormal (QR of seeded
-Gaussians) and sigma geometric from 1 to 1e-6, generated on the device
-(synthetic, seeded).  Before every step A is restored from a pristine copy
+ABI.  Input: A = U diag(sigma) V^T with U, V orthonormal (orthonormalised
+seeded Gaussians) and sigma geometric from 1 to 1e-6, generated on the host
+(numpy, seeded) so that the reference arm factors the identical matrix.  Before every step A is restored from a pristine copy
 and L2 is flushed by writing a 256 MiB buffer; both happen outside the
 per-step CUDA-event pair, so `value` is the device time of the factorisation
 alone, with the input resident in HBM.  A (512 MiB) is itself larger than L2.
@@ -25,6 +25,11 @@ Printed (rank 0, one JSON line):
   reference_protocol  the head form timed the reference's way (20 warm-up
                and 50 timed calls, A copied in from the host before each,
                a device synchronise inside the event pair)
+  suite        the benchmark's other configurations in the same run, each
+               with errors and a roofline fraction: tsqr_n64 (4,194,304 x 64),
+               qr_c1 (27,648 x 128 standard normal, FP32 and FP64), qr_c4
+               (131,072 x 512, condition 1e4, reorthogonalised), batch_c3
+               (512 uneven problems, graph vs loop); --no-suite skips it
 
 --workload batch: 512 uneven FP32 problems through the batched entry point,
 replayed from one CUDA graph, against a loop of single calls (problems/s).
@@ -154,6 +159,29 @@ def orthonormal_columns(G):
         Linv = torch.linalg.inv(torch.linalg.cholesky(C))
         G = G @ Linv.t().to(G.device)
     return G
+
+
+def make_input_host(m, n, seed, kappa=1e6):
+    """The same kind of matrix as make_input, generated on the host with
+    numpy (seeded, platform-independent), so that the GPU arm and the
+    reference arm factor the identical matrix: A = U diag(sigma) V^T with U, V
+    orthonormalised seeded Gaussians (two CholeskyQR passes in FP64) and sigma
+    geometric 1 -> 1/kappa.  FP32, column-major.  Works on the transposes
+    (n x m, row-major), so every product is one BLAS call and the result is
+    column-major without a transposing copy."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+
+    def orth_rows(H):  # rows of H made orthonormal
+        for _ in range(2):
+            L = np.linalg.cholesky(H @ H.T)
+            H = np.linalg.inv(L) @ H
+        return H
+    Ut = orth_rows(rng.standard_normal((n, m)))
+    V = orth_rows(rng.standard_normal((n, n))).T
+    sig = np.logspace(0, -np.log10(kappa), n)
+    At = (V * sig) @ Ut  # A^T = V diag(sigma) U^T
+    return At.astype(np.float32).T
 
 
 def make_input(m, n, seed, device):
@@ -340,13 +368,15 @@ def run_implicit(tg, A0, steps, warmup, device, flush):
             "rel_diff": d.item()}
 
 
-def cpu_port(m, n, budget_s=20.0, seed=0):
-    """The oracle's restatement of the reference TSQR (FP32) on the host."""
+def cpu_port(m, n, budget_s=20.0, A=None):
+    """The oracle's restatement of the reference TSQR (FP32) on the host, on
+    A (the GPU arm's matrix) or the reference's uniform stream."""
     import numpy as np
     from oracle import oracle as orc
     cores = len(os.sched_getaffinity(0))
     orc.set_num_threads(cores)
-    A = orc.fill_uniform(m, n, np.float32, seed=seed)
+    if A is None:
+        A = orc.fill_uniform(m, n, np.float32, seed=0)
     t0 = time.perf_counter()
     reps = 0
     while True:
@@ -357,7 +387,8 @@ def cpu_port(m, n, budget_s=20.0, seed=0):
             break
     sec = el / reps
     return {"value": flops(m, n) / sec / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-            "sample": "full %dx%d FP32 TSQR, %d repetition(s), %.3f s each" % (m, n, reps, sec)}
+            "sample": "full %dx%d FP32 TSQR of the GPU arm's matrix, %d repetition(s), %.3f s each"
+                      % (m, n, reps, sec)}
 
 
 def cpu_lapack(m, n, seed=0):
@@ -426,6 +457,7 @@ def run_batch(tg, steps, warmup, device, seed=2024):
             a.copy_(b)
 
     def capture():
+        stream.wait_stream(torch.cuda.current_stream())  # inputs made on the current stream
         with torch.cuda.stream(stream):
             for _ in range(max(warmup, 1)):
                 restore()
@@ -499,6 +531,7 @@ def run_qr(tg, m, n, dtype, forms, reorth, steps, warmup, device, kappa=1e4, see
             continue
         work = torch.empty(nb, dtype=torch.uint8, device=device)
         stream = torch.cuda.Stream(device=device)
+        stream.wait_stream(torch.cuda.current_stream())  # A0 was made on the current stream
         ts = []
         for k in range(warmup + steps):
             with torch.cuda.stream(stream):
@@ -515,6 +548,180 @@ def run_qr(tg, m, n, dtype, forms, reorth, steps, warmup, device, kappa=1e4, see
         msx = sum(ts) / len(ts)
         out[f] = {"ms": msx, "tflops": flops(m, n) / (msx * 1e-3) / 1e12, "backward": back, "orth": orth}
     return out
+
+
+def _time_calls(fn, restore, steps, warmup, stream, flush=None):
+    """Mean CUDA-event time (ms) of fn() on `stream`, inputs restored (and L2
+    flushed) before every call, outside the event pair."""
+    import torch
+    # the inputs were made on the current stream: order `stream` after them
+    stream.wait_stream(torch.cuda.current_stream())
+    ts = []
+    for k in range(warmup + steps):
+        with torch.cuda.stream(stream):
+            restore()
+            if flush is not None:
+                flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+        stream.synchronize()
+        if k >= warmup:
+            ts.append(a.elapsed_time(b))
+    return sum(ts) / len(ts)
+
+
+def _roof(F, B, ms, pipe_tflops, hbm_gbs):
+    """Roofline of a call: max(F / pipe peak, B / HBM peak), and ms against it."""
+    t = max(F / (pipe_tflops * 1e12), B / (hbm_gbs * 1e9)) * 1e3
+    return {"time_ms": t, "frac": t / ms}
+
+
+def run_extras(tg, device, pk, fp32_peak, steps=5, warmup=2):
+    """The other configurations of the benchmark suite, measured in the same
+    run (compact: a few steps each, errors against FP64 on the device):
+      tsqr_n64  FP32 TSQR 4,194,304 x 64, A = U diag(sigma) V^T (sigma 1..1e-6)
+      qr_c1     blocked QR 27,648 x 128, standard-normal entries, FP32 and FP64
+      qr_c4     blocked QR 131,072 x 512 FP32, condition 1e4, reorthogonalised
+      batch_c3  512 uneven FP32 TSQR problems (one CUDA graph, default table)
+                against a loop of single calls
+    Every figure carries its roofline fraction: FP32 (or nominal FP64) pipe
+    against the measured HBM peak."""
+    import numpy as np
+    import torch
+    fp64_peak = 1.25  # TFLOP/s, nominal GB300 FP64 (no measured figure)
+    hbm = pk["hbm_gbs"]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    stream = torch.cuda.Stream(device=device)
+    out = {}
+
+    def one_tsqr(A0, forms):
+        m, n = A0.shape
+        res = {}
+        for f in forms:
+            A = tg.empty_colmajor(m, n, torch.float32, device)
+            R = tg.empty_colmajor(n, n, torch.float32, device)
+            w = torch.empty(tg.workspace_bytes(m, n, torch.float32, precision=f), dtype=torch.uint8, device=device)
+            ms = _time_calls(lambda: tg.tsqr_(A, R, precision=f, work=w, stream=stream), lambda: A.copy_(A0), steps,
+                             warmup, stream, flush)
+            b, o = check_errors(A0, A, R)
+            res[f] = {"ms": ms, "tflops": flops(m, n) / (ms * 1e-3) / 1e12, "backward": b, "orth": o,
+                      "step_roofline": _roof(flops(m, n), alg_bytes(m, n), ms, fp32_peak, hbm)}
+        return res
+
+    try:
+        A0 = make_input(4194304, 64, 4321, device)
+        out["tsqr_n64"] = {"workload": "TSQR FP32 4194304 x 64, U diag(sigma) V^T, sigma 1..1e-6",
+                           **one_tsqr(A0, ["plain", "tf32x3"])}
+        del A0
+    except Exception as e:  # pragma: no cover
+        out["tsqr_n64"] = {"error": str(e)}
+
+    def one_qr(A0, forms, reorth):
+        m, n = A0.shape
+        dt = A0.dtype
+        res = {}
+        for f in forms:
+            A = A0.t().clone().t()
+            R = tg.empty_colmajor(n, n, dt, device)
+            nb = tg.qr_workspace_bytes(m, n, dt, precision=f, reorth=reorth)
+            w = torch.empty(nb, dtype=torch.uint8, device=device)
+            ms = _time_calls(lambda: tg.qr_(A, R, precision=f, reorth=reorth, work=w, stream=stream),
+                             lambda: A.copy_(A0), steps, warmup, stream, flush)
+            b, o = check_errors(A0, A, R)
+            es = 8 if dt == torch.float64 else 4
+            pipe = fp64_peak if dt == torch.float64 else fp32_peak
+            res[f] = {"ms": ms, "tflops": flops(m, n) / (ms * 1e-3) / 1e12, "backward": b, "orth": o,
+                      "step_roofline": _roof(flops(m, n), alg_bytes(m, n, es), ms, pipe, hbm),
+                      "pipe": "FP64 nominal 1.25 TFLOP/s" if dt == torch.float64 else "FP32 nominal"}
+        return res
+
+    try:
+        g = torch.Generator(device=device).manual_seed(128)
+        N = torch.randn((128, 27648), generator=g, device=device, dtype=torch.float64).t()
+        out["qr_c1"] = {"workload": "blocked QR 27648 x 128, standard-normal entries (seeded)",
+                        "f32": one_qr(N.float().t().contiguous().t(), ["plain", "tf32x3"], False),
+                        "f64": one_qr(N.t().contiguous().t(), ["plain"], False)}
+    except Exception as e:  # pragma: no cover
+        out["qr_c1"] = {"error": str(e)}
+
+    try:
+        m, n = 131072, 512
+        g = torch.Generator(device=device).manual_seed(77)
+        U = orthonormal_columns(torch.randn((m, n), generator=g, device=device, dtype=torch.float64))
+        V = orthonormal_columns(torch.randn((n, n), generator=g, device=device, dtype=torch.float64))
+        sig = torch.logspace(0, -4, n, device=device, dtype=torch.float64)
+        A0 = ((U * sig) @ V.t()).float().t().contiguous().t()
+        del U
+        out["qr_c4"] = {"workload": "blocked QR 131072 x 512 FP32, condition 1e4, one reorthogonalisation pass",
+                        **one_qr(A0, ["plain", "tf32x3"], True)}
+        del A0
+    except Exception as e:  # pragma: no cover
+        out["qr_c4"] = {"error": str(e)}
+
+    try:
+        out["batch_c3"] = run_batch_compact(tg, device, steps, warmup, hbm)
+    except Exception as e:  # pragma: no cover
+        out["batch_c3"] = {"error": str(e)}
+    return out
+
+
+def batch_problems(seed=2024):
+    """The 512 uneven problems: heights log-uniform in [2048, 262144], widths
+    from {8, 16, 32, 64}."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    ms = np.exp(rng.uniform(np.log(2048), np.log(262144), 512)).astype(np.int64)
+    ns = rng.choice([8, 16, 32, 64], 512)
+    return ms, ns
+
+
+def run_batch_compact(tg, device, steps, warmup, hbm_gbs, seed=2024):
+    """The 512-problem batch with the default tile table, one CUDA graph,
+    against a loop of single calls; problems/s, and the graph's algorithmic
+    bytes (sum of (2 m n + n^2) 4) against the HBM peak."""
+    import ctypes
+    import torch
+    ms, ns = batch_problems(seed)
+    g = torch.Generator(device=device).manual_seed(seed)
+    A0 = [torch.rand((int(n), int(m)), generator=g, device=device).mul_(2).sub_(1).t() for m, n in zip(ms, ns)]
+    As = [a.t().clone().t() for a in A0]
+    Rs = [tg.empty_colmajor(int(n), int(n), torch.float32, device) for n in ns]
+    i64 = ctypes.c_int64 * len(As)
+    nbytes = tg.lib().tsqr_batched_workspace_bytes(len(As), i64(*[int(x) for x in ms]), i64(*[int(x) for x in ns]))
+    work = torch.empty(nbytes, dtype=torch.uint8, device=device)
+    stream = torch.cuda.Stream(device=device)
+
+    def restore():
+        for a, b in zip(As, A0):
+            a.copy_(b)
+    stream.wait_stream(torch.cuda.current_stream())  # the inputs were made on the current stream
+    with torch.cuda.stream(stream):
+        restore()
+        tg.tsqr_batched_(As, Rs, work=work, stream=stream)
+    stream.synchronize()
+    gr = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(gr, stream=stream):
+        tg.tsqr_batched_(As, Rs, work=work, stream=stream)
+
+    def loop():
+        for x, r in zip(As, Rs):
+            tg.tsqr_(x, r, stream=stream)
+    t_graph = _time_calls(gr.replay, restore, steps, warmup, stream)
+    t_loop = _time_calls(loop, restore, max(2, steps // 2), 1, stream)
+    B = float(sum((2.0 * int(m) * int(n) + int(n) ** 2) * 4 for m, n in zip(ms, ns)))
+    F = float(sum(flops(int(m), int(n)) for m, n in zip(ms, ns)))
+    back = []
+    for k in range(0, 512, 64):
+        a0, q, r = A0[k].double(), As[k].double(), Rs[k].double()
+        back.append((torch.linalg.norm(a0 - q @ r) / torch.linalg.norm(a0)).item())
+    return {"workload": "512 uneven FP32 problems, heights log-uniform [2048, 262144], widths {8,16,32,64}, "
+                        "uniform[-1,1), one CUDA graph, default tile table",
+            "graph_ms": t_graph, "problems_per_s": 512 / (t_graph * 1e-3), "loop_ms": t_loop,
+            "graph_vs_loop": t_loop / t_graph, "tflops": F / (t_graph * 1e-3) / 1e12,
+            "algorithmic_bytes": B, "achieved_gbs": B / (t_graph * 1e-3) / 1e9,
+            "hbm_frac": B / (t_graph * 1e-3) / 1e9 / hbm_gbs, "max_backward_sampled": max(back)}
 
 
 def dist_env():
@@ -554,6 +761,8 @@ def main():
     ap.add_argument("--n", "--cols", dest="n", type=int, default=32)
     ap.add_argument("--form", default="auto")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-suite", action="store_true", help="skip the other configurations (tsqr_n64, qr_c1, "
+                                                            "qr_c4, batch_c3)")
     ap.add_argument("--workload", default="tsqr", choices=["tsqr", "batch", "qr"])
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"], help="qr workload only")
     ap.add_argument("--reorth", action="store_true", help="qr workload: one reorthogonalisation pass")
@@ -570,11 +779,11 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        t = cpu_port(m, n, budget_s=1e9)  # each step a full factorisation
-        times = []
         import numpy as np
         from oracle import oracle as orc
-        A = orc.fill_uniform(m, n, np.float32)
+        A = make_input_host(m, n, 1234)  # the GPU arm's matrix (rank 0)
+        t = cpu_port(m, n, budget_s=1e9, A=A)  # each step a full factorisation
+        times = []
         for _ in range(min(args.warmup, 1)):
             orc.ref_tsqr(A)
         for _ in range(args.steps):
@@ -585,8 +794,10 @@ def main():
         val = F / sec / 1e12
         out = {"metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f32", "data": "synthetic: reference input stream (uniform[-1,1), "
-               "std::default_random_engine(0))", "impl": "reference",
+               "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic: A = U diag(sigma) V^T, U,V orthonormalised seeded Gaussians, sigma geometric "
+                       "1..1e-6, generated on the host (numpy, seed 1234): the GPU arm's matrix",
+               "impl": "reference",
                "config": {"workload": workload, "parallelism": "host cores, OpenMP over row chunks"},
                "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": t["cores"], "kind": "port",
                                 "sample": "full %dx%d FP32 TSQR per step" % (m, n)},
@@ -658,7 +869,9 @@ def main():
             dist.destroy_process_group()
         return 0
 
-    A0 = make_input(m, n, 1234 + rank, device)
+    A_host = make_input_host(m, n, 1234 + rank)
+    A0 = tg.empty_colmajor(m, n, torch.float32, device)
+    A0.copy_(torch.from_numpy(A_host))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
     forms = ["plain", "tf32x3"] if args.form == "auto" else [args.form]
     results = {}
@@ -701,9 +914,10 @@ def main():
     implicit = run_implicit(tg, A0, max(3, args.steps // 4), 2, device, flush)
     e2e["ms"] = max_over_ranks(e2e["ms"], ws, device)
     e2e_val = whole_job_rate(F, e2e["ms"], ws) / 1e12
+    suite = None if args.no_suite else run_extras(tg, device, pk, fp32_peak)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu = cpu_port(m, n)
+        cpu = cpu_port(m, n, A=A_host)
         lap = cpu_lapack(m, n)
     else:
         lap = None
@@ -712,7 +926,8 @@ def main():
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: A = U diag(sigma) V^T, U,V from QR of seeded Gaussians, sigma geometric 1..1e-6",
+        "data": "synthetic: A = U diag(sigma) V^T, U,V orthonormalised seeded Gaussians, sigma geometric 1..1e-6, "
+                "generated on the host (numpy, seed 1234 + rank), the same matrix the reference arm factors",
         "config": {"workload": workload, "form": head, "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "flushed (256 MiB write) before every step; A (%d MiB) > L2" % (m * n * 4 >> 20),
                    "input_restore": "A restored from a pristine copy before every step, outside the timed pair"},
@@ -729,7 +944,7 @@ def main():
                 "d2h_bytes_per_step": e2e["d2h"], "ms_per_step": e2e["ms"],
                 "api": "tsqr_s_host (pinned host A in, Q and R out; copies pipelined with the level-0 kernels)",
                 "backward": e2e["backward"], "orth": e2e["orth"]},
-        "implicit_q": implicit, "reference_protocol": ref_protocol,
+        "implicit_q": implicit, "reference_protocol": ref_protocol, "suite": suite,
         "cpu_baseline": cpu, "cpu_lapack": lap,
         "clocks": clocks, "gpu_launches": nl * args.steps, "launches_per_step": nl,
         "forms": {f: ({"ms": v["ms"], "tflops": F / (v["ms"] * 1e-3) / 1e12, "backward": v["backward"],

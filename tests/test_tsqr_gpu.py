@@ -240,3 +240,62 @@ def test_matches_reference_cuda_golden(orc, cuda, tg, name):
     u = orc.unit_roundoff(dtype)
     assert np.abs(R - Rg).max() <= 100 * n * u * np.abs(Rg).max()
     assert np.abs(Q[d["q_idx"]] - qg).max() <= 100 * n * u
+
+
+@pytest.mark.parametrize("n", [32, 64])
+@pytest.mark.parametrize("form", ["plain", "tf32x3"])
+def test_tsqr_full_size_conditioned_input(orc, cuda, tg, n, form):
+    """The 4,194,304-row workload as the benchmark states it: A = U diag(sigma)
+    V^T with U, V orthonormalised seeded Gaussians and sigma geometric from 1
+    to 1e-6 (condition 1e6).  Size-independent properties in FP64 on the
+    device: backward error and orthogonality within the form's bar (plain:
+    10 n u; tf32x3: 1e-5), R upper triangular."""
+    import torch
+    m = 4194304
+    g = torch.Generator(device="cuda").manual_seed(6 + n)
+
+    def orth(G):
+        for _ in range(2):
+            L = torch.linalg.cholesky(G.t() @ G)
+            G = torch.linalg.solve_triangular(L, G.t(), upper=False).t()
+        return G
+    U = orth(torch.randn((m, n), generator=g, device="cuda", dtype=torch.float64))
+    V = orth(torch.randn((n, n), generator=g, device="cuda", dtype=torch.float64))
+    sig = torch.logspace(0, -6, n, device="cuda", dtype=torch.float64)
+    A0 = ((U * sig) @ V.t()).float().t().contiguous().t()
+    del U
+    A = A0.t().clone().t()
+    R = tg.tsqr_(A, precision=form)
+    torch.cuda.synchronize()
+    back, orthf = gpu_metrics(A0, A, R)
+    bar = 10 * n * 2.0 ** -24 if form == "plain" else 1e-5
+    assert back <= bar and orthf <= bar, (back, orthf)
+    assert torch.all(torch.tril(R, -1) == 0)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("form", ["plain", "tf32x3"])
+def test_blocked_qr_standard_normal_input(orc, cuda, tg, dtype, form):
+    """The blocked-QR configuration as stated: 27,648 x 128 with i.i.d.
+    standard-normal entries from a seed, in FP32 (both forms) and FP64
+    (plain).  Against the oracle's FP64 figures (10 n u; tf32x3 1e-5) and
+    against the oracle's restatement of the reference qr after diag(R) >= 0."""
+    if dtype == np.float64 and form != "plain":
+        pytest.skip("the precision form is FP32 only")
+    m, n = 27648, 128
+    rng = np.random.default_rng(128)
+    A = np.asfortranarray(rng.standard_normal((m, n)).astype(dtype))
+    dA = to_dev(tg, A)
+    dR = tg.qr_(dA, precision=form)
+    Q, R = to_host(dA), to_host(dR)
+    u = orc.unit_roundoff(dtype)
+    met = orc.metrics(A, Q, R)
+    bar = 10 * n * u if form == "plain" else 1e-5
+    assert met["backward"] <= bar and met["orth"] <= bar, met
+    Qr, Rr = orc.ref_qr(A)
+    Qs, Rs = np.asfortranarray(Q.astype(np.float64)), np.asfortranarray(R.astype(np.float64))
+    Qr, Rr = np.asfortranarray(Qr.astype(np.float64)), np.asfortranarray(Rr.astype(np.float64))
+    orc.sign_fix(Qs, Rs)
+    orc.sign_fix(Qr, Rr)
+    tol = 1000 * n * u if form == "plain" else 1e-4
+    assert np.abs(Rs - Rr).max() <= tol * np.abs(Rr).max()
