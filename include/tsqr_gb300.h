@@ -43,8 +43,11 @@ typedef enum tsqr_precision {
     TSQR_PRECISION_PLAIN = 0,   /* working precision on CUDA cores (FP32 or FP64) */
     TSQR_PRECISION_TF32X3 = 1,  /* FP32 entry points only: tcgen05 TF32 hi/lo
                                    3-product split, FP32 accumulation in TMEM  */
-    TSQR_PRECISION_BF16X3 = 2   /* FP32 entry points only: tcgen05 BF16 hi/lo
-                                   3-product split, FP32 accumulation in TMEM  */
+    TSQR_PRECISION_BF16X3 = 2   /* qr_s_ex only: its GEMMs on tcgen05 with BF16
+                                   hi/lo 3-product splits (about 2^-16 relative
+                                   per product), FP32 accumulation in TMEM; its
+                                   TSQR panels run TF32X3.  tsqr_* entry points
+                                   return TSQR_ERR_UNSUPPORTED                 */
 } tsqr_precision;
 
 /* Algorithm of qr_*_ex. */

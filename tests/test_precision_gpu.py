@@ -260,3 +260,36 @@ def test_tsqr_reorthogonalisation_pass(orc, cuda, tg, form, dtype, m, n):
     assert np.abs(R - R1).max() <= tol * np.abs(R1).max()
     if form == "tf32x3":
         assert tg.lib().tsqr_workspace_check(w.data_ptr()) == 0
+
+
+@pytest.mark.parametrize("algorithm", ["block_gs", "householder"])
+def test_bf16x3_blocked_qr(orc, cuda, tg, algorithm):
+    """TSQR_PRECISION_BF16X3 for qr: the GEMMs on tcgen05 with BF16 hi/lo
+    three-product splits (each product carries about 2^-16 relative error,
+    against 2^-21 for TF32x3); the TSQR panels run TF32x3.  Bar: backward
+    error <= 1e-5 against FP64, orthogonality <= 5e-4 (block Gram-Schmidt on
+    a standard-normal matrix; the Householder algorithm stays near 1e-5), and
+    R within 1e-4 max|R| of the TF32x3 form's."""
+    import torch
+    m, n = 27648, 128
+    rng = np.random.default_rng(129)
+    A = np.asfortranarray(rng.standard_normal((m, n)).astype(np.float32))
+    out = {}
+    for prec in ("bf16x3", "tf32x3"):
+        dA = to_dev(tg, A)
+        w = torch.zeros(tg.qr_workspace_bytes(m, n, torch.float32, precision=prec, algorithm=algorithm),
+                        dtype=torch.uint8, device="cuda")
+        dR = tg.qr_(dA, precision=prec, algorithm=algorithm, work=w)
+        torch.cuda.synchronize()
+        assert tg.lib().tsqr_workspace_check(w.data_ptr()) == 0
+        out[prec] = (to_host(dA), to_host(dR))
+    Q, R = out["bf16x3"]
+    met = orc.metrics(A, Q, R)
+    orth_bar = 5e-4 if algorithm == "block_gs" else 1e-4
+    assert met["backward"] <= 1e-5 and met["orth"] <= orth_bar, met
+    R32 = out["tf32x3"][1]
+    Rs, R32s = np.asfortranarray(R.astype(np.float64)), np.asfortranarray(R32.astype(np.float64))
+    Qs, Q32s = np.asfortranarray(Q.astype(np.float64)), np.asfortranarray(out["tf32x3"][0].astype(np.float64))
+    orc.sign_fix(Qs, Rs)
+    orc.sign_fix(Q32s, R32s)
+    assert np.abs(Rs - R32s).max() <= 1e-4 * np.abs(R32s).max()

@@ -119,7 +119,6 @@ tsqr_status qr_ex(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, vo
     tsqr_status st = check_common<T>(m, n, A, lda, R, ldr, o);
     if (st != TSQR_OK) return st;
     if (o.panel > max_tsqr_n<T>() || o.fp64_scalars || o.fp64_root) return TSQR_ERR_UNSUPPORTED;
-    if (sizeof(T) == 4 && o.precision == TSQR_PRECISION_BF16X3) return TSQR_ERR_UNSUPPORTED;
     return tsqr::qr_run<T>(m, n, A, lda, R, ldr, work, work_bytes, o, (cudaStream_t)stream);
 }
 

@@ -212,9 +212,15 @@ struct QrWs {
     size_t total() const { return err_bytes + tsqr_bytes + part_bytes + tmp_bytes; }
 };
 
+// The tensor-core forms (FP32 only): TF32X3, or BF16X3, whose GEMMs use
+// BF16 hi/lo splits (the TSQR panels stay on the TF32x3 tensor-core form).
 template <typename T>
 bool use_tc(const tsqr_opts& o) {
-    return sizeof(T) == 4 && o.precision == TSQR_PRECISION_TF32X3;
+    return sizeof(T) == 4 && (o.precision == TSQR_PRECISION_TF32X3 || o.precision == TSQR_PRECISION_BF16X3);
+}
+template <typename T>
+bool use_bf16(const tsqr_opts& o) {
+    return sizeof(T) == 4 && o.precision == TSQR_PRECISION_BF16X3;
 }
 
 // The projection R12 = A1^T A2 runs on the tensor cores only when both sides
@@ -241,9 +247,9 @@ void qr_ws_walk(int64_t m, int64_t n, int nb, bool reorth, bool tc, QrWs* w) {
 // C (n1 x n2, ldc) = A1^T A2 (+ beta C) on the tensor cores (FP32 only).
 template <typename T>
 void proj_tn_tc(int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2, int64_t lda, T* P, T* C, int64_t ldc,
-                T beta, int* err, cudaStream_t s) {
+                T beta, int* err, cudaStream_t s, bool bf16) {
     if constexpr (std::is_same<T, float>::value) {
-        const int nz = tc_gemm_tn((int)n1, (int)n2, m, A1, lda, A2, lda, P, err, s);
+        const int nz = tc_gemm_tn((int)n1, (int)n2, m, A1, lda, A2, lda, P, err, s, bf16);
         log_launch(kTagTc + 100, s);
         const int64_t total = n1 * n2;
         int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 1024);
@@ -255,9 +261,9 @@ void proj_tn_tc(int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2, int
 // A2 (m x n2) -= A1 (m x n1) X (n1 x n2) on the tensor cores (FP32 only).
 template <typename T>
 void update_nn_tc(int64_t m, int64_t n1, int64_t n2, const T* A1, int64_t lda, const T* X, int64_t ldx, T* A2,
-                  int* err, cudaStream_t s) {
+                  int* err, cudaStream_t s, bool bf16) {
     if constexpr (std::is_same<T, float>::value) {
-        tc_gemm_nn(m, (int)n2, (int)n1, -1.f, A1, lda, X, ldx, A2, lda, err, s);
+        tc_gemm_nn(m, (int)n2, (int)n1, -1.f, A1, lda, X, ldx, A2, lda, err, s, bf16);
         log_launch(kTagTc + 101, s);
     }
 }
@@ -303,10 +309,10 @@ tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, c
     const bool tcp = tc_projection(tc, n1, n2);
     if (tc) {
         if (tcp)
-            proj_tn_tc<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), err, s);
+            proj_tn_tc<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), err, s, use_bf16<T>(o));
         else
             proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), s);
-        update_nn_tc<T>(m, n1, n2, A1, lda, R12, ldr, A2, err, s);
+        update_nn_tc<T>(m, n1, n2, A1, lda, R12, ldr, A2, err, s, use_bf16<T>(o));
     } else {
         proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), s);
         gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, R12, ldr, T(1), A2, lda);
@@ -315,10 +321,10 @@ tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, c
     if (o.reorth) {
         if (tc) {
             if (tcp)
-                proj_tn_tc<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), err, s);
+                proj_tn_tc<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), err, s, use_bf16<T>(o));
             else
                 proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), s);
-            update_nn_tc<T>(m, n1, n2, A1, lda, tmp, n1, A2, err, s);
+            update_nn_tc<T>(m, n1, n2, A1, lda, tmp, n1, A2, err, s, use_bf16<T>(o));
         } else {
             proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), s);
             gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, tmp, n1, T(1), A2, lda);
@@ -543,6 +549,7 @@ struct HqrCtx {
     T *part, *Rp, *Uinv, *Mb, *W, *X;
     int* err;
     bool tc;
+    bool bf16 = false;  // BF16x3 tensor-core GEMMs
     int b;
     cudaStream_t s;
 };
@@ -555,7 +562,7 @@ inline unsigned grid_of(int64_t work, int64_t cap) {
 template <typename T>
 void hqr_tn(const HqrCtx<T>& c, int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2, T* C) {
     if (tc_projection(c.tc, n1, n2))
-        proj_tn_tc<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.err, c.s);
+        proj_tn_tc<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.err, c.s, c.bf16);
     else
         proj_tn<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.s);
 }
@@ -564,7 +571,7 @@ void hqr_tn(const HqrCtx<T>& c, int64_t m, int64_t n1, int64_t n2, const T* A1, 
 template <typename T>
 void hqr_nn(const HqrCtx<T>& c, int64_t m, int64_t n1, int64_t n2, const T* Y, const T* X, T* A2) {
     if (c.tc) {
-        update_nn_tc<T>(m, n1, n2, Y, c.lda, X, n1, A2, c.err, c.s);
+        update_nn_tc<T>(m, n1, n2, Y, c.lda, X, n1, A2, c.err, c.s, c.bf16);
     } else {
         dim3 g((unsigned)ceil_div(m, kTile), (unsigned)ceil_div(n2, kTile));
         gemm_nn<T><<<g, 256, 0, c.s>>>(m, (int)n2, (int)n1, T(-1), Y, c.lda, X, n1, T(1), A2, c.lda);
@@ -670,6 +677,7 @@ tsqr_status hqr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, 
     c.X = reinterpret_cast<T*>(sm + w.small + w.wx / 2);
     T* Tfull = reinterpret_cast<T*>(sm + w.small + w.wx);
     c.tc = tc;
+    c.bf16 = use_bf16<T>(o);
     c.b = b;
     c.s = s;
     if (tc && cudaMemsetAsync(c.err, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;

@@ -157,12 +157,13 @@ tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R
 }  // namespace tsqr
 
 namespace tsqr {
-// tcgen05 TF32x3 GEMMs of the blocked QR precision form (tc_gemm.cu).
+// tcgen05 GEMMs of the blocked QR precision forms (tc_gemm.cu): TF32x3, or
+// BF16x3 with bf16 = true.
 int tc_tn_splits(int64_t M, int64_t N, int64_t K);
 int tc_gemm_tn(int M, int N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb, float* P, int* err,
-               cudaStream_t s);
+               cudaStream_t s, bool bf16 = false);
 void tc_gemm_nn(int64_t M, int N, int K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb,
-                float* C, int64_t ldc, int* err, cudaStream_t s);
+                float* C, int64_t ldc, int* err, cudaStream_t s, bool bf16 = false);
 }  // namespace tsqr
 
 namespace tsqr {

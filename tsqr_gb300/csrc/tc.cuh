@@ -45,6 +45,29 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
            | ((uint32_t)(M >> 4) << 24);   // M / 16
 }
 
+// Instruction descriptor, kind::f16 with BF16 A and B (both the same type),
+// FP32 accumulator, both K-major, M x N tile.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4)                       // D format F32
+           | (1u << 7)                     // A format BF16
+           | (1u << 10)                    // B format BF16
+           | ((uint32_t)(N >> 3) << 17)    // N / 8
+           | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+// D[tmem] (+)= A[smem] * B[smem], BF16 operands (K = 16), issued by one thread.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         bool accumulate) {
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "setp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"((uint32_t)accumulate)
+        : "memory");
+}
+
 // D[tmem] (+)= A[smem] * B[smem], issued by one thread.
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          bool accumulate) {
@@ -134,6 +157,19 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
 __device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
     hi = to_tf32(x);
     lo = to_tf32(x - __uint_as_float(hi));
+}
+
+// BF16 split: hi = x rounded to BF16 (nearest even), lo = the remainder
+// rounded to BF16; hi*hi + hi*lo + lo*hi keeps about 2^-16 relative of an
+// FP32 product (the BF16x3 form).  Returned as the 16-bit patterns.
+__device__ __forceinline__ uint32_t to_bf16(float x) {
+    unsigned short h;
+    asm("cvt.rn.bf16.f32 %0, %1;\n" : "=h"(h) : "f"(x));
+    return (uint32_t)h;
+}
+__device__ __forceinline__ void split_bf16(float x, uint32_t& hi, uint32_t& lo) {
+    hi = to_bf16(x);
+    lo = to_bf16(x - __uint_as_float(hi << 16));
 }
 
 }  // namespace tc

@@ -43,7 +43,10 @@ struct GemmSmem {
     uint32_t tmem_slot;
 };
 
-template <bool TRANS_A, int NB>
+// BF: BF16x3 instead of TF32x3 -- the same K-major tiles hold 16-bit
+// values (a core matrix row = 8 values of K), and each MMA (kind::f16, both
+// operands BF16) covers K = 16.
+template <bool TRANS_A, int NB, bool BF = false>
 __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, const float* __restrict__ A, int64_t lda,
                                                       const float* __restrict__ Bm, int64_t ldb, float* __restrict__ C,
                                                       int64_t ldc,
@@ -51,8 +54,13 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
     extern __shared__ __align__(1024) unsigned char gemm_smem_raw[];
     GemmSmem<NB>& S = *reinterpret_cast<GemmSmem<NB>*>(gemm_smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
-    constexpr uint32_t idesc = tc::idesc_tf32(128, NB);
-    constexpr uint32_t SBO = KS * 32;  // bytes per 8-row group of a K-major tile with K = KS
+    constexpr uint32_t idesc = BF ? tc::idesc_bf16(128, NB) : tc::idesc_tf32(128, NB);
+    constexpr uint32_t ES = BF ? 2 : 4;          // operand element bytes
+    constexpr uint32_t SBO = KS * 8 * ES;        // bytes per 8-row group of a K-major tile with K = KS
+    // byte offset of element (row, k) of a K-major no-swizzle tile with K = KS
+    auto koff = [](int row, int k) -> uint32_t {
+        return (uint32_t)((row >> 3) * SBO + (k * ES / 16) * 128 + (row & 7) * 16 + (k * ES) % 16);
+    };
 
     const int m0 = blockIdx.x * 128;
     const int n0 = blockIdx.y * NB;
@@ -75,6 +83,24 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
 
     // Stage s: K rows [k0, k0 + KS).  A operand rows = output rows m, B
     // operand rows = output columns n, both K-major (KS values per row).
+    // four consecutive K values of one operand row, split into hi and lo
+    auto store_split = [](unsigned char* hp, unsigned char* lp, uint32_t off, const float(&v)[4]) {
+        if constexpr (BF) {
+            uint32_t h[4], l[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) tc::split_bf16(v[e], h[e], l[e]);
+            *reinterpret_cast<uint2*>(hp + off) = make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16));
+            *reinterpret_cast<uint2*>(lp + off) = make_uint2(l[0] | (l[1] << 16), l[2] | (l[3] << 16));
+        } else {
+            uint4 hi, lo;
+            tc::split_tf32(v[0], hi.x, lo.x);
+            tc::split_tf32(v[1], hi.y, lo.y);
+            tc::split_tf32(v[2], hi.z, lo.z);
+            tc::split_tf32(v[3], hi.w, lo.w);
+            *reinterpret_cast<uint4*>(hp + off) = hi;
+            *reinterpret_cast<uint4*>(lp + off) = lo;
+        }
+    };
     auto stage = [&](int s, int buf) {
         const int64_t k0 = kbeg + (int64_t)s * KS;
         unsigned char* ah = reinterpret_cast<unsigned char*>(S.a_hi[buf]);
@@ -124,14 +150,7 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
                 row = task % 128;
                 k4 = (task / 128) * 4;
             }
-            uint4 hi, lo;
-            tc::split_tf32(va[it][0], hi.x, lo.x);
-            tc::split_tf32(va[it][1], hi.y, lo.y);
-            tc::split_tf32(va[it][2], hi.z, lo.z);
-            tc::split_tf32(va[it][3], hi.w, lo.w);
-            const uint32_t off = tc::kmajor_off(row, k4, KS);
-            *reinterpret_cast<uint4*>(ah + off) = hi;
-            *reinterpret_cast<uint4*>(al + off) = lo;
+            store_split(ah, al, koff(row, k4), va[it]);
         }
         // B: NB rows (output columns) x KS; element (n, k) = Bm[k + n*ldb],
         // in rounds of at most 8 tasks per thread (loads, then stores).
@@ -159,14 +178,7 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
                 const int grp = task >> 5;
                 const int row = (grp % (NB / 8)) * 8 + (task & 7);
                 const int k4 = ((grp / (NB / 8)) * 4 + ((task >> 3) & 3)) * 4;
-                uint4 hi, lo;
-                tc::split_tf32(vb[it][0], hi.x, lo.x);
-                tc::split_tf32(vb[it][1], hi.y, lo.y);
-                tc::split_tf32(vb[it][2], hi.z, lo.z);
-                tc::split_tf32(vb[it][3], hi.w, lo.w);
-                const uint32_t off = tc::kmajor_off(row, k4, KS);
-                *reinterpret_cast<uint4*>(bh + off) = hi;
-                *reinterpret_cast<uint4*>(bl + off) = lo;
+                store_split(bh, bl, koff(row, k4), vb[it]);
             }
         }
         tc::fence_smem_to_async();
@@ -174,14 +186,21 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
     auto issue = [&](int s, int buf) {
         const uint32_t ah = tc::smem_u32(S.a_hi[buf]), al = tc::smem_u32(S.a_lo[buf]);
         const uint32_t bh = tc::smem_u32(S.b_hi[buf]), bl = tc::smem_u32(S.b_lo[buf]);
+        // one MMA covers 32 bytes of K: 8 TF32 or 16 BF16 values
 #pragma unroll
-        for (int ks = 0; ks < KS / 8; ++ks) {
+        for (int ks = 0; ks < KS * (int)ES / 32; ++ks) {
             const uint32_t ko = ks * 256;
             const uint64_t dah = tc::smem_desc(ah + ko, 128, SBO), dal = tc::smem_desc(al + ko, 128, SBO);
             const uint64_t dbh = tc::smem_desc(bh + ko, 128, SBO), dbl = tc::smem_desc(bl + ko, 128, SBO);
-            tc::mma_tf32(tmem, dah, dbh, idesc, (s > 0) || (ks > 0));
-            tc::mma_tf32(tmem, dah, dbl, idesc, true);
-            tc::mma_tf32(tmem, dal, dbh, idesc, true);
+            if constexpr (BF) {
+                tc::mma_bf16(tmem, dah, dbh, idesc, (s > 0) || (ks > 0));
+                tc::mma_bf16(tmem, dah, dbl, idesc, true);
+                tc::mma_bf16(tmem, dal, dbh, idesc, true);
+            } else {
+                tc::mma_tf32(tmem, dah, dbh, idesc, (s > 0) || (ks > 0));
+                tc::mma_tf32(tmem, dah, dbl, idesc, true);
+                tc::mma_tf32(tmem, dal, dbh, idesc, true);
+            }
         }
         tc::mma_commit(tc::smem_u32(&S.mbar[buf]));
     };
@@ -277,16 +296,28 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
     if (warp == 0) tc::tmem_dealloc(tmem, NB);
 }
 
-template <bool TRANS_A, int NB>
+template <bool TRANS_A, int NB, bool BF>
 void launch_gemm(dim3 grid, int M, int N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
                  float* C, int64_t ldc, float alpha, int64_t kchunk, int* err, cudaStream_t s) {
     constexpr size_t smem = sizeof(GemmSmem<NB>) + 1024;
     static PerDeviceOnce attr;
     attr.run([] {
-        cudaFuncSetAttribute(tc_gemm_kernel<TRANS_A, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(tc_gemm_kernel<TRANS_A, NB, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
     });
-    tc_gemm_kernel<TRANS_A, NB><<<grid, 128, smem, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err,
-                                                         wait_tries().load(std::memory_order_relaxed));
+    tc_gemm_kernel<TRANS_A, NB, BF><<<grid, 128, smem, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err,
+                                                             wait_tries().load(std::memory_order_relaxed));
+}
+
+template <bool TRANS_A, bool BF>
+void launch_nb(int nb, dim3 g, int M, int N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
+               float* C, int64_t ldc, float alpha, int64_t kchunk, int* err, cudaStream_t s) {
+    switch (nb) {
+        case 32: launch_gemm<TRANS_A, 32, BF>(g, M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err, s); break;
+        case 64: launch_gemm<TRANS_A, 64, BF>(g, M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err, s); break;
+        case 128: launch_gemm<TRANS_A, 128, BF>(g, M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err, s); break;
+        default: launch_gemm<TRANS_A, 256, BF>(g, M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err, s); break;
+    }
 }
 
 int nb_for(int N) { return N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256)); }
@@ -301,35 +332,33 @@ int tc_tn_splits(int64_t M, int64_t N, int64_t K) {
 }
 
 // P_z = A^T B over K-chunks (M, N <= 256 per launch dimension); P holds
-// nz * M * N floats.  Returns the number of partial sums written.
+// nz * M * N floats.  Returns the number of partial sums written.  bf16:
+// BF16x3 products instead of TF32x3.
 int tc_gemm_tn(int M, int N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb, float* P, int* err,
-               cudaStream_t s) {
+               cudaStream_t s, bool bf16) {
     const int nz = tc_tn_splits(M, N, K);
     int64_t kchunk = (K + nz - 1) / nz;
     kchunk = (kchunk + KS - 1) / KS * KS;
     const int nzr = (int)((K + kchunk - 1) / kchunk);
     const int nb = nb_for(std::min(N, 256));
     dim3 g((unsigned)((M + 127) / 128), (unsigned)((N + nb - 1) / nb), (unsigned)nzr);
-    switch (nb) {
-        case 32: launch_gemm<true, 32>(g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s); break;
-        case 64: launch_gemm<true, 64>(g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s); break;
-        case 128: launch_gemm<true, 128>(g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s); break;
-        default: launch_gemm<true, 256>(g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s); break;
-    }
+    if (bf16)
+        launch_nb<true, true>(nb, g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s);
+    else
+        launch_nb<true, false>(nb, g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s);
     return nzr;
 }
 
-// C (M x N) += alpha * A (M x K) * B (K x N), K and N small (<= 256 per N block).
+// C (M x N) += alpha * A (M x K) * B (K x N), K and N small (<= 256 per N
+// block).  bf16: BF16x3 products instead of TF32x3.
 void tc_gemm_nn(int64_t M, int N, int K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb,
-                float* C, int64_t ldc, int* err, cudaStream_t s) {
+                float* C, int64_t ldc, int* err, cudaStream_t s, bool bf16) {
     const int nb = nb_for(std::min(N, 256));
     dim3 g((unsigned)((M + 127) / 128), (unsigned)((N + nb - 1) / nb), 1);
-    switch (nb) {
-        case 32: launch_gemm<false, 32>(g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s); break;
-        case 64: launch_gemm<false, 64>(g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s); break;
-        case 128: launch_gemm<false, 128>(g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s); break;
-        default: launch_gemm<false, 256>(g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s); break;
-    }
+    if (bf16)
+        launch_nb<false, true>(nb, g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s);
+    else
+        launch_nb<false, false>(nb, g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s);
 }
 
 }  // namespace tsqr
