@@ -137,7 +137,11 @@ tsqr_status qr_float(int m, int n, float* A, int lda, float* R, int ldr, float* 
 tsqr_status qr_double(int m, int n, double* A, int lda, double* R, int ldr, double* d_work, int ldwork);
 
 /* Batched TSQR: `count` independent problems of uneven heights m[i] and
- * widths n[i] (FP32, n[i] <= 64), factored by one persistent launch.  The
+ * widths n[i] (FP32, n[i] <= 64).  The problems are grouped by (width class,
+ * tile configuration); each group takes one factor launch per tree level
+ * and one apply launch per level, persistent CTAs walking the group's tiles
+ * from a per-problem table passed by value -- no host-to-device copy and no
+ * allocation, so the whole call can be captured into one CUDA graph.  The
  * pointer/size arrays are HOST arrays; A[i], R[i] are device pointers.  No
  * counterpart in the reference (which factors one matrix per call). */
 size_t tsqr_batched_workspace_bytes(int count, const int64_t* m, const int64_t* n);
