@@ -92,12 +92,14 @@ tsqr_status tsqr_s_ex(int64_t m, int64_t n, float* A, int64_t lda, float* R, int
 tsqr_status tsqr_d_ex(int64_t m, int64_t n, double* A, int64_t lda, double* R, int64_t ldr,
                       void* work, size_t work_bytes, const tsqr_opts* opts, void* stream);
 
-/* Tensor-core status of a TF32X3 call (tsqr_s_ex, tsqr_s_host, qr_s_ex)
+/* Status of a call (TF32X3: tsqr_s_ex, tsqr_s_host, qr_s_ex)
  * after it has completed: the tcgen05 kernels bound every wait on their
  * mbarriers; one that runs out stops the kernel and sets a status word in
  * the first 4 bytes of the call's workspace.  Returns TSQR_OK, or
  * TSQR_ERR_CUDA when that word is set (the results are then incomplete).
- * Reads 4 bytes with a synchronous copy; not meaningful for PLAIN calls. */
+ * PLAIN TSQR calls (tsqr_*_ex, tsqr_*_factor, tsqr_*_host) keep such a word
+ * too, for the bounded wait of their TMA-fed tile factor.  Reads 4 bytes
+ * with a synchronous copy. */
 tsqr_status tsqr_workspace_check(const void* work);
 
 /* TSQR of a matrix in host memory, with Q and R returned to host memory:

@@ -34,6 +34,11 @@ KNOWN = {
     "tsqr::factor_split_tiles<float, 64, 8, 8, 1, true>": (68, 68),
     "tsqr::factor_split_tiles<float, 64, 8, 4, 1, true>": (4, 4),
     "tsqr::factor_split_tiles<float, 64, 8, 2, 1, true>": (4, 4),
+    # the TMA-staged tile factor: 8 bytes (two registers) of its loop state
+    # at the 128-register limit of 2 CTAs per SM; measured at parity with the
+    # register-load kernel on the level it serves
+    "tsqr::factor_split_tiles_tma<float, 32, 4, 16, 2>": (8, 8),
+    "tsqr::factor_split_tiles_tma<float, 16, 4, 16, 4>": (8, 8),
     # batched kernels: per-problem descriptors cost registers
     "tsqr::batched_apply<64, 256, 2, 1>": (88, 128),
     "tsqr::batched_apply<32, 256, 2, 2>": (80, 112),

@@ -146,6 +146,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, int tr
     return false;
 }
 
+// TMA: announce `bytes` of transactions on an mbarrier (and arrive once).
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
+}
+// TMA: 2D tiled load of the box at coordinates (x, y) of the tensor map into
+// shared memory, completing as transactions on `mbar`.  x (the innermost,
+// contiguous coordinate) times the element size must be a multiple of 16.
+__device__ __forceinline__ void tma_load_2d(uint32_t smem_dst, const void* tmap, int x, int y, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];\n" ::"r"(smem_dst),
+        "l"(tmap), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
+}
+
 // TF32 split: hi = x rounded to TF32 (round to nearest, ties away), lo = the
 // rounded remainder.  hi*hi + hi*lo + lo*hi reproduces an FP32 product to
 // about 2^-21 relative.

@@ -23,6 +23,41 @@ thread_local LaunchLog* tl_log = nullptr;
 
 namespace {
 
+// cuTensorMapEncodeTiled, looked up once through the runtime (no link
+// against the driver library).  Null if the driver does not offer it.
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        (void)cudaGetLastError();
+        return reinterpret_cast<EncodeTiledFn>(f);
+    }();
+    return fn;
+}
+
+// Tensor map of an FP32 level matrix (h rows x n columns, leading dimension
+// ld) for boxes of 256 rows x nbox columns; rows >= h and columns >= n read
+// as zeros.  False when the matrix does not meet TMA's rules (16-byte base,
+// ld a multiple of 4 floats).
+bool level_tensor_map(CUtensorMap* map, const float* M, int64_t ld, int64_t h, int n, int nbox) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc || (reinterpret_cast<uintptr_t>(M) % 16) != 0 || ld % 4 != 0 || h < 1) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
+    const cuuint32_t box[2] = {256u, (cuuint32_t)nbox};
+    const cuuint32_t estr[2] = {1u, 1u};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(M), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <typename T, int NMAX, int NT, int RPT, int MINB, int AMINB, int ANT = NT, bool NORM64 = false>
 struct TileCfg {
     static_assert((NT * RPT) % ANT == 0, "apply block must divide the tile");
@@ -61,6 +96,27 @@ struct SplitCfg {
             if (p.ntiles == 1 && p.h <= 128) return factor_split_tiles<T, NMAX, CW, 4, 1, N64><<<1, W32, 0, s>>>(p);
         if constexpr (RPT > 8)
             if (p.ntiles == 1 && p.h <= 256) return factor_split_tiles<T, NMAX, CW, 8, 1, N64><<<1, W32, 0, s>>>(p);
+        if constexpr (std::is_same<T, float>::value && RPT == 16 && NMAX <= 32 && !N64) {
+            // levels with several tiles per resident CTA: tiles staged by TMA
+            // into shared memory, the next one copied while the current one
+            // is factored (persistent CTAs).  Measured at 4,194,304 x 32:
+            // level 0 0.670 ms against 0.667 ms with register loads, so the
+            // staging costs nothing there; levels of one wave or less were
+            // 2 us slower with it and keep the plain loads.
+            const int64_t resident = (int64_t)device_sm_count() * MINB;
+            CUtensorMap map;
+            if (p.ntiles >= 2 * resident && p.ntiles * kRows <= INT32_MAX &&
+                level_tensor_map(&map, p.M, p.ld, p.h, p.n, NMAX)) {
+                constexpr size_t smem = tma_stage_bytes<T, NMAX, CW, RPT>();
+                static PerDeviceOnce attr;
+                attr.run([] {
+                    cudaFuncSetAttribute(factor_split_tiles_tma<T, NMAX, CW, RPT, MINB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                });
+                const int g = (int)std::min<int64_t>(p.ntiles, resident);
+                return factor_split_tiles_tma<T, NMAX, CW, RPT, MINB><<<g, W32, smem, s>>>(p, map);
+            }
+        }
         factor_split_tiles<T, NMAX, CW, RPT, MINB, N64><<<grid, W32, 0, s>>>(p);
     }
     static void apply(const ApplyParams<T>& p, int grid, cudaStream_t s) {
@@ -137,12 +193,14 @@ size_t plan_levels(int64_t m, int64_t n, T* A, int64_t lda, int rows, char* base
 
 }  // namespace
 
+// Workspace of the plain tree: a status word (256 bytes; non-zero after a
+// factor kernel's bounded wait gave up, read by tsqr_workspace_check), then
+// the level matrices.
 template <typename T>
 size_t tsqr_plain_workspace(int64_t m, int64_t n) {
     KernelSet<T> ks = pick((T*)nullptr, (int)n);
     if (!ks.factor) return 0;
-    size_t b = plan_levels<T>(m, n, nullptr, m, ks.rows, nullptr, nullptr);
-    return b ? b : kAlign;  // never report 0 for a valid size
+    return kAlign + plan_levels<T>(m, n, nullptr, m, ks.rows, nullptr, nullptr);
 }
 
 template <typename T>
@@ -151,8 +209,13 @@ tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ld
     KernelSet<T> ks = pick((T*)nullptr, (int)n);
     if (!ks.factor) return TSQR_ERR_UNSUPPORTED;
     std::vector<Level<T>> lv;
-    size_t need = plan_levels<T>(m, n, A, lda, ks.rows, reinterpret_cast<char*>(work), &lv);
-    if (need > 0 && (work == nullptr || work_bytes < need)) return TSQR_ERR_WORKSPACE;
+    char* wb = reinterpret_cast<char*>(work);
+    size_t need = plan_levels<T>(m, n, A, lda, ks.rows, wb ? wb + kAlign : nullptr, &lv);
+    if (need > 0 && (work == nullptr || work_bytes < kAlign + need)) return TSQR_ERR_WORKSPACE;
+    // a single-tile problem may run without a workspace, and then without a
+    // status word
+    int* err = (work != nullptr && work_bytes >= kAlign) ? reinterpret_cast<int*>(work) : nullptr;
+    if (err && (phases & kPhaseUp) && cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
     const int L = (int)lv.size();
     // up-sweep
     for (int l = 0; l < L && (phases & kPhaseUp); ++l) {
@@ -162,6 +225,7 @@ tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ld
         fp.h = lv[l].h;
         fp.n = (int)n;
         fp.ntiles = lv[l].ntiles;
+        fp.err = err;
         if (l == L - 1) {
             fp.Rout = R;
             fp.ldr = ldr;
@@ -298,6 +362,7 @@ tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R
         fp.h = lv[l].h;
         fp.n = (int)n;
         fp.ntiles = lv[l].ntiles;
+        fp.err = err;
         fp.Rout = (l == L - 1) ? R : lv[l + 1].M;
         fp.ldr = (l == L - 1) ? ldr : lv[l + 1].ld;
         c.ks.factor(fp, (int)std::min<int64_t>(lv[l].ntiles, 1 << 30), s);
@@ -353,9 +418,9 @@ tsqr_status tsqr_plain_tree(int64_t m, int64_t n, const T* A, int64_t lda, const
     KernelSet<T> ks = pick((T*)nullptr, (int)n);
     if (!ks.factor) return TSQR_ERR_UNSUPPORTED;
     std::vector<Level<T>> lv;
-    size_t need = plan_levels<T>(m, n, const_cast<T*>(A), lda, ks.rows,
-                                 const_cast<char*>(reinterpret_cast<const char*>(work)), &lv);
-    if (need > 0 && (work == nullptr || work_bytes < need)) return TSQR_ERR_WORKSPACE;
+    char* wb = const_cast<char*>(reinterpret_cast<const char*>(work));
+    size_t need = plan_levels<T>(m, n, const_cast<T*>(A), lda, ks.rows, wb ? wb + kAlign : nullptr, &lv);
+    if (need > 0 && (work == nullptr || work_bytes < kAlign + need)) return TSQR_ERR_WORKSPACE;
     out->clear();
     for (const Level<T>& v : lv) out->push_back({v.M, v.ld, v.h, v.ntiles, ks.rows});
     return TSQR_OK;
@@ -473,7 +538,11 @@ tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int
             lvbase = tw + PL.levels;
         }
     }
-    if (!prec) ks = pick((T*)nullptr, (int)n);
+    if (!prec) {
+        ks = pick((T*)nullptr, (int)n);
+        err = reinterpret_cast<int*>(tw);  // the plain tree's status word
+        lvbase = tw + kAlign;
+    }
     if (!ks.factor) return TSQR_ERR_UNSUPPORTED;
     std::vector<Level<T>> lv;
     plan_levels<T>(m, n, dA, HL.ldd, ks.rows, lvbase, &lv);
@@ -487,6 +556,7 @@ tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int
         fp.h = std::min<int64_t>(cnt * rows, lv[l].h - t0 * rows);
         fp.n = (int)n;
         fp.ntiles = cnt;
+        fp.err = err;
         fp.Rout = (l == L - 1) ? dR : lv[l + 1].M + t0 * n;
         fp.ldr = (l == L - 1) ? n : lv[l + 1].ld;
         ks.factor(fp, (int)std::min<int64_t>(cnt, 1 << 30), s);

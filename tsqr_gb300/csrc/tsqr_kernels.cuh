@@ -38,7 +38,10 @@
 #pragma once
 #include <type_traits>
 
+#include <cuda.h>  // CUtensorMap (the type only; no driver calls here)
+
 #include "common.cuh"
+#include "tc.cuh"
 
 namespace tsqr {
 
@@ -51,6 +54,7 @@ struct FactorParams {
     int64_t ntiles;
     T* Rout;        // R of tile t goes to rows [t*n, t*n+n) of Rout
     int64_t ldr;
+    int* err = nullptr;  // status word: set to 1 when a bounded wait gives up (null: none)
 };
 
 template <typename T>
@@ -385,8 +389,8 @@ struct Vec16;
 template <>
 struct Vec16<float> {
     static constexpr int N = 4;
-    __device__ static void store(float* p, const float* v) { *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]); }
-    __device__ static void load(const float* p, float* v) {
+    __device__ __forceinline__ static void store(float* p, const float* v) { *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]); }
+    __device__ __forceinline__ static void load(const float* p, float* v) {
         const float4 q = *reinterpret_cast<const float4*>(p);
         v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
     }
@@ -394,8 +398,8 @@ struct Vec16<float> {
 template <>
 struct Vec16<double> {
     static constexpr int N = 2;
-    __device__ static void store(double* p, const double* v) { *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]); }
-    __device__ static void load(const double* p, double* v) {
+    __device__ __forceinline__ static void store(double* p, const double* v) { *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]); }
+    __device__ __forceinline__ static void load(const double* p, double* v) {
         const double2 q = *reinterpret_cast<const double2*>(p);
         v[0] = q.x, v[1] = q.y;
     }
@@ -422,9 +426,9 @@ struct VbufLayout {
     static constexpr int VN = Vec16<T>::N;
     static constexpr int KC = RPT / VN;
     static constexpr bool kVec = VEC && (RPT % VN == 0) && KC >= 1 && KC <= 8 && (KC & (KC - 1)) == 0;
-    __device__ static int swz(int lane) { return kVec ? (lane / (8 / KC)) & (KC - 1) : 0; }
+    __device__ __forceinline__ static int swz(int lane) { return kVec ? (lane / (8 / KC)) & (KC - 1) : 0; }
     template <typename F>
-    __device__ static void store(T* buf, int lane, int sw, F&& val) {
+    __device__ __forceinline__ static void store(T* buf, int lane, int sw, F&& val) {
         if constexpr (kVec) {
 #pragma unroll
             for (int k = 0; k < KC; ++k) {
@@ -438,7 +442,7 @@ struct VbufLayout {
             for (int i = 0; i < RPT; ++i) buf[lane + 32 * i] = val(i);
         }
     }
-    __device__ static void load(const T* buf, int lane, int sw, T (&v)[RPT]) {
+    __device__ __forceinline__ static void load(const T* buf, int lane, int sw, T (&v)[RPT]) {
         if constexpr (kVec) {
 #pragma unroll
             for (int k = 0; k < KC; ++k) Vec16<T>::load(buf + lane * RPT + VN * (k ^ sw), &v[k * VN]);
@@ -502,9 +506,18 @@ __device__ __forceinline__ T warp_colsum(const T (&q)[CW], T* scratch, int lane)
 // the reflector scalars beta, tau and 1/(alpha - beta) in FP64, rounded to
 // the tile's type once computed; the tile, the dot products and the updates
 // stay in T.  (The precision form's option fp64_scalars.)
-template <typename T, int NMAX, int CW, int RPT, bool VECV = (NMAX <= 32), bool N64 = false>
+// The tile comes from global memory (Hook = NoHook), or from a copy in
+// shared memory staged by TMA (any other Hook; stile): 256-row boxes of
+// NMAX columns, box h holding rows [256h, 256h + 256) column by column, the
+// rows past the level's end and the columns past n already zero.  `loaded`
+// runs once every thread holds its values.
+struct NoHook {
+    __device__ __forceinline__ void operator()() const {}
+};
+template <typename T, int NMAX, int CW, int RPT, bool VECV = (NMAX <= 32), bool N64 = false, class Hook = NoHook>
 __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, RPT>& S, T* tile, int64_t ld, int ht,
-                                                  int n, T* Rt, int64_t ldr) {
+                                                  int n, T* Rt, int64_t ldr, const T* stile = nullptr,
+                                                  Hook loaded = Hook()) {
     using SC = typename std::conditional<N64, double, T>::type;  // type of the reflector scalars
     constexpr int W = NMAX / CW;
     constexpr int U = 4;
@@ -539,7 +552,14 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
     };
 
     T y[RPT][CW];
-    {
+    if constexpr (!std::is_same<Hook, NoHook>::value) {
+        // rows lane + 32 i of box i / 8, consecutive lanes on consecutive words
+        const T* s0 = stile + col0 * 256 + lane;
+#pragma unroll
+        for (int c = 0; c < CW; ++c)
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) y[i][c] = s0[((i >> 3) * NMAX + c) * 256 + 32 * (i & 7)];
+    } else {
         // one column pointer stepped by ld; the row offsets 32*i are immediates
         const T* pcol = tile + (int64_t)col0 * ld + lane;
 #pragma unroll
@@ -549,6 +569,7 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
             pcol += ld;
         }
     }
+    loaded();
     int shift = 0;  // after this warp's own phase, position c holds its local column (c + shift) % CW
 
 #pragma unroll 1
@@ -739,6 +760,92 @@ __global__ void __launch_bounds__(32 * (NMAX / CW), MINB) factor_split_tiles(Fac
         const int64_t row0 = t * B;
         const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
         factor_split_tile<T, NMAX, CW, RPT, (NMAX <= 32), N64>(S, p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n, p.ldr);
+    }
+}
+
+// Persistent form of factor_split_tiles whose tiles are staged into shared
+// memory by TMA (two 256-row boxes of a 512-row tile, rows past the level's
+// end filled with zeros by the copy itself): a CTA waits for its tile, every
+// thread takes its values into registers, and the TMA of the CTA's next tile
+// is issued while the current one is factored, so the tile load leaves the
+// tile's chain.  The wait is bounded: after tc::kMbarTries polls the CTA
+// sets the status word, waits (bounded) for the copy in flight and stops.
+// Dynamic shared memory of the TMA form: the tile's boxes, then the
+// mbarrier that counts their bytes (both at fixed offsets, so neither
+// address takes a register across the tile).
+extern __shared__ __align__(128) unsigned char tma_stage[];
+template <typename T, int NMAX, int CW, int RPT>
+constexpr size_t tma_tile_bytes() {
+    return (size_t)(RPT / 8) * NMAX * 256 * sizeof(T);
+}
+template <typename T, int NMAX, int CW, int RPT>
+constexpr size_t tma_stage_bytes() {
+    return tma_tile_bytes<T, NMAX, CW, RPT>() + 16;
+}
+// One thread: the copies of the tile whose first row is y, counted on the
+// stage's mbarrier.
+template <int BOXES, int BOX_BYTES>
+__device__ __forceinline__ void tma_issue_tile(const CUtensorMap* tmap, int y) {
+    const uint32_t dst = tc::smem_u32(tma_stage), mb = dst + BOXES * BOX_BYTES;
+    tc::fence_smem_to_async();
+    tc::mbar_arrive_expect_tx(mb, (uint32_t)(BOXES * BOX_BYTES));
+#pragma unroll
+    for (int h = 0; h < BOXES; ++h) tc::tma_load_2d(dst + h * BOX_BYTES, tmap, y + h * 256, 0, mb);
+}
+// The `loaded` hook of the TMA form: every thread holds its values, so the
+// buffer is free and thread 0 (go) starts the next tile's copy.  Held by
+// value: a hook that referred to the loop's locals would put them on the
+// stack.
+template <int BOXES, int BOX_BYTES>
+struct TmaNextTile {
+    const CUtensorMap* tmap;
+    int y;
+    bool go;
+    __device__ __forceinline__ void operator()() const {
+        __syncthreads();
+        if (go) tma_issue_tile<BOXES, BOX_BYTES>(tmap, y);
+    }
+};
+template <typename T, int NMAX, int CW, int RPT, int MINB>
+__global__ void __launch_bounds__(32 * (NMAX / CW), MINB)
+    factor_split_tiles_tma(FactorParams<T> p, const __grid_constant__ CUtensorMap tmap) {
+    static_assert(RPT % 8 == 0, "tiles of whole 256-row boxes");
+    constexpr int B = 32 * RPT, BOXES = RPT / 8, BOX_BYTES = NMAX * 256 * (int)sizeof(T);
+    __shared__ SplitFactorSmem<T, NMAX, CW, RPT> S;
+    const T* stile = reinterpret_cast<const T*>(tma_stage);
+    const uint32_t mb = tc::smem_u32(tma_stage) + BOXES * BOX_BYTES;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(mb, 1);
+        tc::fence_mbar_init();
+    }
+    __syncthreads();
+    // Row coordinates fit 32 bits (TMA takes them signed; the host launches
+    // this kernel for ntiles * B <= INT32_MAX only).  The loop carries one
+    // counter k (tile
+    // blockIdx.x + k gridDim.x, mbarrier phase k & 1) across the tile's
+    // body, which needs every register it can get.
+    const int ntiles = (int)p.ntiles;
+    if (threadIdx.x == 0 && (int)blockIdx.x < ntiles)
+        tma_issue_tile<BOXES, BOX_BYTES>(&tmap, (int)blockIdx.x * B);
+#pragma unroll 1
+    for (int k = 0;; ++k) {
+        const int t = (int)blockIdx.x + k * (int)gridDim.x;
+        if (t >= (int)p.ntiles) break;
+        const uint32_t phase = (uint32_t)k & 1u;
+        const bool ok = tc::mbar_wait(mb, phase);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                if (p.err) atomicExch(p.err, 1);
+                (void)tc::mbar_wait(mb, phase);  // the copy in flight must not land after the CTA is gone
+            }
+            break;
+        }
+        const int64_t row0 = (int64_t)t * B;
+        const int ht = (int)((p.h - row0) < B ? (p.h - row0) : B);
+        const int tn = t + (int)gridDim.x;
+        const TmaNextTile<BOXES, BOX_BYTES> loaded{&tmap, tn * B, threadIdx.x == 0 && tn < (int)p.ntiles};
+        factor_split_tile<T, NMAX, CW, RPT, (NMAX <= 32), false>(S, p.M + row0, p.ld, ht, p.n, p.Rout + t * p.n,
+                                                                  p.ldr, stile, loaded);
     }
 }
 
