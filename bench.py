@@ -60,7 +60,7 @@ METRIC = "QR TFLOP/s & % roofline, tensor-core vs plain FP32 at equal FP64-oracl
 # level-0 kernels at 4,194,304 x 32: one ncu --set full capture of each kernel
 # at 2,097,152 rows (factor 494.6 MB, tensor-core apply 492.8 MB, CUDA-core
 # apply 492.2 MB), scaled by the tile count (x2).
-TRAFFIC = {(4194304, 32, "factor_level0"): 2 * 492.4e6,
+TRAFFIC = {(4194304, 32, "factor_level0"): 2 * 493.6e6,
            (4194304, 32, "tc_level0"): 2 * 492.5e6,
            (4194304, 32, "apply_level0"): 2 * 492.2e6}
 TRAFFIC_SOURCE = "ncu capture at 2,097,152 rows, x2 for the tile count"

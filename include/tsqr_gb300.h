@@ -258,15 +258,17 @@ const char* tsqr_status_string(tsqr_status s);
 /* Library version, e.g. "0.1.0". */
 const char* tsqr_version(void);
 
-/* Test hook for the failure path of the tensor-core kernels (no counterpart
- * in the reference, whose grid barrier spins without a limit,
- * kernelQR.h:374).  Sets how many times the tcgen05 kernels of later calls
- * (tc_apply_tiles, tc_gemm_kernel) poll an mbarrier for their MMAs before
- * giving up; 0 makes the first wait of every such kernel give up at once, so
+/* Test hook for the failure path of the kernels that wait on an mbarrier
+ * (no counterpart in the reference, whose grid barrier spins without a
+ * limit, kernelQR.h:374).  Sets how many times the kernels of later calls
+ * poll an mbarrier before giving up: the tcgen05 kernels (tc_apply_tiles,
+ * tc_gemm_kernel) for their MMAs, and the TMA-staged tile factor for its
+ * tile.  0 makes the first wait of every such kernel give up at once, so
  * the call's status word is set and tsqr_workspace_check reports
  * TSQR_ERR_CUDA.  The waits that let in-flight MMAs retire before TMEM is
- * freed always keep the full limit.  polls < 0 restores the default
- * (2^24 polls, seconds).  Process-wide; for tests only. */
+ * freed, or in-flight copies land before a CTA exits, always keep the full
+ * limit.  polls < 0 restores the default (2^24 polls, seconds).
+ * Process-wide; for tests only. */
 tsqr_status tsqr_debug_set_wait_limit(int polls);
 
 #ifdef __cplusplus

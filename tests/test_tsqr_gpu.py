@@ -96,6 +96,46 @@ def test_reference_signature_form(orc, cuda, tg):
     check_against_oracle(orc, A, to_host(dA), to_host(dR))
 
 
+# The FP32 tile factor for 9 <= n <= 32 stages its tiles into shared memory
+# by TMA on levels with at least two tiles per resident CTA (152 SMs x 2 CTAs
+# at n > 16, x 4 at n <= 16).  These shapes take that path: a ragged last
+# tile (rows past m zero-filled by the copy), columns past n inside the
+# 16/32-column box, a padded leading dimension; and one whose leading
+# dimension is not a multiple of 4 floats, which keeps the register loads.
+@pytest.mark.parametrize("m,n,ld_pad", [(311297, 32, 3), (700001, 16, 3), (650000, 20, 0), (700000, 9, 0),
+                                        (400001, 32, 0)])
+def test_tma_staged_tile_factor(orc, cuda, tg, m, n, ld_pad):
+    A = orc.fill_uniform(m, n, np.float32, seed=41)
+    dA = to_dev(tg, A, ld_pad=ld_pad)
+    dR = tg.tsqr_(dA)
+    check_against_oracle(orc, A, to_host(dA), to_host(dR))
+
+
+def test_tma_tile_wait_that_runs_out_is_reported(orc, cuda, tg):
+    """The TMA-staged tile factor's wait for its tile, limited to 0 polls
+    (tsqr_debug_set_wait_limit), gives up at once: each CTA sets the call's
+    status word, lets its copy in flight land and stops.  The next call with
+    the default limit succeeds and clears the word."""
+    import torch
+    L = tg.lib()
+    m, n = 400000, 32
+    A = orc.fill_uniform(m, n, np.float32, seed=42)
+    w = torch.zeros(tg.workspace_bytes(m, n, torch.float32), dtype=torch.uint8, device="cuda")
+    try:
+        assert L.tsqr_debug_set_wait_limit(0) == 0
+        tg.tsqr_(to_dev(tg, A), work=w)
+        torch.cuda.synchronize()
+        assert L.tsqr_workspace_check(w.data_ptr()) == 4  # TSQR_ERR_CUDA
+    finally:
+        L.tsqr_debug_set_wait_limit(-1)
+    torch.cuda.synchronize()
+    dA = to_dev(tg, A)
+    dR = tg.tsqr_(dA, work=w)
+    torch.cuda.synchronize()
+    assert L.tsqr_workspace_check(w.data_ptr()) == 0
+    check_against_oracle(orc, A, to_host(dA), to_host(dR))
+
+
 def test_results_are_deterministic(orc, cuda, tg):
     A = orc.fill_uniform(200000, 32, np.float32, seed=7)
     outs = []

@@ -226,6 +226,7 @@ tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ld
         fp.n = (int)n;
         fp.ntiles = lv[l].ntiles;
         fp.err = err;
+        fp.tries = wait_tries().load(std::memory_order_relaxed);
         if (l == L - 1) {
             fp.Rout = R;
             fp.ldr = ldr;
@@ -363,6 +364,7 @@ tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R
         fp.n = (int)n;
         fp.ntiles = lv[l].ntiles;
         fp.err = err;
+        fp.tries = wait_tries().load(std::memory_order_relaxed);
         fp.Rout = (l == L - 1) ? R : lv[l + 1].M;
         fp.ldr = (l == L - 1) ? ldr : lv[l + 1].ld;
         c.ks.factor(fp, (int)std::min<int64_t>(lv[l].ntiles, 1 << 30), s);
@@ -557,6 +559,7 @@ tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int
         fp.n = (int)n;
         fp.ntiles = cnt;
         fp.err = err;
+        fp.tries = wait_tries().load(std::memory_order_relaxed);
         fp.Rout = (l == L - 1) ? dR : lv[l + 1].M + t0 * n;
         fp.ldr = (l == L - 1) ? n : lv[l + 1].ld;
         ks.factor(fp, (int)std::min<int64_t>(cnt, 1 << 30), s);

@@ -55,6 +55,7 @@ struct FactorParams {
     T* Rout;        // R of tile t goes to rows [t*n, t*n+n) of Rout
     int64_t ldr;
     int* err = nullptr;  // status word: set to 1 when a bounded wait gives up (null: none)
+    int tries = tc::kMbarTries;  // polls of a bounded wait before it gives up
 };
 
 template <typename T>
@@ -768,8 +769,8 @@ __global__ void __launch_bounds__(32 * (NMAX / CW), MINB) factor_split_tiles(Fac
 // end filled with zeros by the copy itself): a CTA waits for its tile, every
 // thread takes its values into registers, and the TMA of the CTA's next tile
 // is issued while the current one is factored, so the tile load leaves the
-// tile's chain.  The wait is bounded: after tc::kMbarTries polls the CTA
-// sets the status word, waits (bounded) for the copy in flight and stops.
+// tile's chain.  The wait is bounded: after p.tries polls the CTA sets the
+// status word, waits (with the full limit) for the copy in flight and stops.
 // Dynamic shared memory of the TMA form: the tile's boxes, then the
 // mbarrier that counts their bytes (both at fixed offsets, so neither
 // address takes a register across the tile).
@@ -832,11 +833,13 @@ __global__ void __launch_bounds__(32 * (NMAX / CW), MINB)
         const int t = (int)blockIdx.x + k * (int)gridDim.x;
         if (t >= (int)p.ntiles) break;
         const uint32_t phase = (uint32_t)k & 1u;
-        const bool ok = tc::mbar_wait(mb, phase);
+        const bool ok = tc::mbar_wait(mb, phase, p.tries);
         if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) {
                 if (p.err) atomicExch(p.err, 1);
-                (void)tc::mbar_wait(mb, phase);  // the copy in flight must not land after the CTA is gone
+                // the copy in flight must not land after the CTA is gone:
+                // this wait keeps the full limit
+                (void)tc::mbar_wait(mb, phase);
             }
             break;
         }
