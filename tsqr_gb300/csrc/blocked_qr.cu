@@ -5,9 +5,12 @@
 // with TSQR on panels of width <= panel (32, the reference's N_B,
 // block_QR.h:5).  The reference's single naive kernel gemm_blockqr
 // (block_QR.h:7-60: one thread per output, a length-m dot with stride-lda
-// loads for op=T) becomes two tiled SIMT kernels:
-//   gemm_tn_partial + reduce_partials: R12 = A1^T A2, K = m split across
-//     CTAs into deterministic partial sums (no atomics), then summed;
+// loads for op=T) becomes tiled SIMT kernels:
+//   gemm_tn_fused (FP32): R12 = A1^T A2 in 32 x 32 output tiles, K = m split
+//     across CTAs, the partial sums reduced in the same launch in a fixed
+//     order (deterministic);
+//   gemm_tn_partial + reduce_partials (FP64): the same product as split-K
+//     partials of 64 x 64 tiles, then their sum;
 //   gemm_nn: A2 = A2 - A1 R12, streamed over row blocks.
 // Options the reference lacks: any split point (not only n/2 with
 // (n/2) % 32 == 0, block_QR.h:78-79), a second projection (CGS2) when
@@ -90,18 +93,398 @@ __global__ void __launch_bounds__(256) gemm_tn_partial(int M, int N, int64_t K, 
         }
 }
 
-// C = alpha * sum_z P_z + beta * C  (C is M x N with ldc)
+// C = alpha * sum_z P_z + beta * C  (C is M x N with ldc).  A CTA of 8
+// warps takes 32 consecutive elements: warp w sums the partials z = w, w+8,
+// ... of its lane's element (32 independent chains per warp, loads
+// coalesced), then warp 0 adds the 8 warp sums in warp order, so the result
+// is deterministic.
 template <typename T>
-__global__ void reduce_partials(int M, int N, int nz, const T* __restrict__ P, T alpha, T beta, T* C,
-                                int64_t ldc) {
+__global__ void __launch_bounds__(256) reduce_partials(int M, int N, int nz, const T* __restrict__ P, T alpha,
+                                                       T beta, T* C, int64_t ldc) {
+    __shared__ T s[8][32];
     const int64_t total = (int64_t)M * N;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        T s = 0;
-        for (int z = 0; z < nz; ++z) s += P[(int64_t)z * total + e];
-        const int i = (int)(e % M), j = (int)(e / M);
-        T* c = C + i + (int64_t)j * ldc;
-        *c = (beta == T(0)) ? alpha * s : alpha * s + beta * *c;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int64_t base = (int64_t)blockIdx.x * 32; base < total; base += (int64_t)gridDim.x * 32) {
+        const int64_t e = base + lane;
+        T a0 = T(0), a1 = T(0);
+        if (e < total) {
+            int z = w;
+            for (; z + 8 < nz; z += 16) {
+                a0 += P[(int64_t)z * total + e];
+                a1 += P[(int64_t)(z + 8) * total + e];
+            }
+            if (z < nz) a0 += P[(int64_t)z * total + e];
+        }
+        s[w][lane] = a0 + a1;
+        __syncthreads();
+        if (w == 0 && e < total) {
+            T t = s[0][lane];
+#pragma unroll
+            for (int q = 1; q < 8; ++q) t += s[q][lane];
+            const int i = (int)(e % M), j = (int)(e / M);
+            T* c = C + i + (int64_t)j * ldc;
+            *c = (beta == T(0)) ? alpha * t : alpha * t + beta * *c;
+        }
+        __syncthreads();
+    }
+}
+inline int reduce_blocks(int64_t total) { return (int)std::min<int64_t>(ceil_div(total, 32), 4096); }
+
+// ---------------------------------------------------------------------------
+// FP32 projection in one launch: C (n1 x n2, ldc) = alpha A^T B + beta C for
+// A (K x n1) and B (K x n2), column-major.  The output is cut in 32 x 32
+// tiles, so a 32-wide node computes no padding.  The K rows are split into S
+// chunks per tile, one CTA each.  A CTA stages 64 rows of its 32 + 32
+// columns per step in shared memory and reduces the step over four K slices
+// of 64 threads (4 x 4 outputs per thread, 16-byte shared-memory reads).
+// Its partial tile goes to global memory.  The last CTA of each group of g
+// chunks to arrive (an atomic counter) sums the group's partials, and the
+// last group sums the group partials into C.  Both sums run in a fixed order,
+// so the result does not depend on which CTA arrives last.  No CTA waits on
+// another; the last one resets the tile's counters for the next launch.
+constexpr int kPT = 32;      // output tile edge
+constexpr int kPRows = 64;   // rows staged per step
+constexpr int kPCounters = 256 / sizeof(int);  // counter words start here in the workspace header
+constexpr int kPHeader = 4096;                 // status word + counters
+constexpr int kPMaxCounters = kPHeader / (int)sizeof(int) - kPCounters;
+
+struct TnFusedPlan {
+    int tiles_i = 1, ntiles = 1, S = 1, g = 1, G = 1;
+    int64_t kchunk = 0;
+    size_t part_bytes() const {  // chunk partials, then group partials
+        return S > 1 ? (size_t)ntiles * (S + G) * kPT * kPT * sizeof(float) : 0;
+    }
+};
+
+TnFusedPlan tn_fused_plan(int64_t n1, int64_t n2, int64_t K) {
+    TnFusedPlan p;
+    p.tiles_i = (int)ceil_div(n1, kPT);
+    p.ntiles = p.tiles_i * (int)ceil_div(n2, kPT);
+    // one wave of three CTAs per SM on GB300's 152 SMs (the register limit
+    // of 256 threads at 75 registers), chunks of whole 64-row steps.  The
+    // workspace query uses the same plan, so it takes the constant rather
+    // than the device's count.
+    const int64_t want = std::max<int64_t>(1, (3 * 152) / p.ntiles);
+    p.kchunk = round_up(ceil_div(K, std::min<int64_t>(want, ceil_div(K, kPRows))), kPRows);
+    p.S = (int)ceil_div(K, p.kchunk);
+    p.g = 1;
+    while ((int64_t)p.g * p.g < p.S) ++p.g;
+    p.G = (int)ceil_div(p.S, p.g);
+    if (p.S > 1 && (int64_t)p.ntiles * (p.G + 1) > kPMaxCounters) {  // too many counters: one chunk per tile
+        p.S = 1;
+        p.kchunk = round_up(std::max<int64_t>(K, 1), kPRows);
+        p.g = p.G = 1;
+    }
+    return p;
+}
+
+struct TnFusedArgs {
+    int n1, n2;
+    int64_t K;
+    const float* A;
+    const float* B;
+    int64_t ld;  // A and B share it
+    float* C;
+    int64_t ldc;
+    float alpha, beta;
+    int tiles_i, S, g, G;
+    int64_t kchunk;
+    float* part;  // [ntiles][S][1024]
+    float* gpart;  // [ntiles][G][1024]
+    int* cnt;      // [ntiles][G + 1], zero between launches
+};
+
+// sum over z < n of q[z * 256] (float4 elements), in order of z, read from
+// L2 (other CTAs wrote them): eight loads in flight per thread, the sum
+// order unchanged (a missing term adds an exact zero)
+__device__ __forceinline__ float4 sum_partials(const float4* q, int n) {
+    constexpr int kStride = kPT * kPT / 4;
+    float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int z0 = 0; z0 < n; z0 += 8) {
+        float4 w[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+            w[e] = z0 + e < n ? __ldcg(q + (int64_t)(z0 + e) * kStride) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) u.x += w[e].x, u.y += w[e].y, u.z += w[e].z, u.w += w[e].w;
+    }
+    return u;
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(256, 3) gemm_tn_fused(TnFusedArgs p) {
+    __shared__ __align__(16) float sm[2 * kPRows * kPT];  // A step | B step; later the four K slices' tiles
+    __shared__ int s_last;
+    float* As = sm;
+    float* Bs = sm + kPRows * kPT;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tile = blockIdx.x, chunk = blockIdx.y;
+    const int i0 = (tile % p.tiles_i) * kPT, j0 = (tile / p.tiles_i) * kPT;
+    const int64_t kbeg = (int64_t)chunk * p.kchunk;
+    const int64_t kend = min(p.K, kbeg + p.kchunk);
+
+    // Loader: slot e of a thread covers rows 4kq..4kq+3 of one column gc of
+    // the step (gc < 32: A's column i0 + gc, else B's column j0 + gc - 32);
+    // a warp's slot is 4 columns x 32 rows, each column one 128-byte line.
+    // Row r of column c is stored at [r][((c/4) ^ (r/4 % 8)) * 4 + c % 4]:
+    // the stores of a warp hit 32 distinct banks, and a 16-byte read of 4
+    // consecutive columns stays contiguous.
+    const int kqa = lane & 7;
+    const float* src[2];
+    bool colok[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int gc = 4 * (warp * 2 + h) + (lane >> 3);
+        const bool isA = gc < kPT;
+        const int c = isA ? i0 + gc : j0 + gc - kPT;
+        colok[h] = c < (isA ? p.n1 : p.n2);
+        src[h] = (isA ? p.A : p.B) + (int64_t)(colok[h] ? c : 0) * p.ld;
+    }
+    float4 r[4];
+    auto fetch = [&](int64_t k0) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int64_t row = k0 + 4 * (8 * (e & 1) + kqa);
+            const float* q = src[e >> 1] + row;
+            if (!colok[e >> 1]) {
+                r[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+            } else if (VEC && row + 3 < kend) {
+                r[e] = __ldg(reinterpret_cast<const float4*>(q));
+            } else {
+                r[e].x = row < kend ? __ldg(q) : 0.f;
+                r[e].y = row + 1 < kend ? __ldg(q + 1) : 0.f;
+                r[e].z = row + 2 < kend ? __ldg(q + 2) : 0.f;
+                r[e].w = row + 3 < kend ? __ldg(q + 3) : 0.f;
+            }
+        }
+    };
+
+    // compute: slice sl takes rows 16 sl .. 16 sl + 15 of each step; thread
+    // (ig, jg) of the slice owns rows 4ig.. and columns 4jg.. of the tile
+    const int sl = tid >> 6, lt = tid & 63, ig = lt >> 3, jg = lt & 7;
+    float acc[4][4] = {};
+    if (kbeg < kend) fetch(kbeg);
+    for (int64_t k0 = kbeg; k0 < kend; k0 += kPRows) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int kq = 8 * (e & 1) + kqa;
+            const int gc = 4 * (warp * 2 + (e >> 1)) + (lane >> 3);
+            float* dst = (gc < kPT ? As : Bs) + ((((gc & 31) >> 2) ^ (kq & 7)) << 2) + (gc & 3);
+            dst[(4 * kq + 0) * kPT] = r[e].x;
+            dst[(4 * kq + 1) * kPT] = r[e].y;
+            dst[(4 * kq + 2) * kPT] = r[e].z;
+            dst[(4 * kq + 3) * kPT] = r[e].w;
+        }
+        __syncthreads();
+        if (k0 + kPRows < kend) fetch(k0 + kPRows);
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk) {
+            const int k = 16 * sl + kk, s = (k >> 2) & 7;
+            const float4 a = *reinterpret_cast<const float4*>(As + k * kPT + ((ig ^ s) << 2));
+            const float4 b = *reinterpret_cast<const float4*>(Bs + k * kPT + ((jg ^ s) << 2));
+            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+        }
+        __syncthreads();
+    }
+
+    // the four slices' tiles, column-major (element j*32 + i), summed in
+    // slice order by the thread that owns elements 4t..4t+3
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+        *reinterpret_cast<float4*>(sm + sl * kPT * kPT + (4 * jg + v) * kPT + 4 * ig) =
+            make_float4(acc[0][v], acc[1][v], acc[2][v], acc[3][v]);
+    __syncthreads();
+    float4 t = *reinterpret_cast<const float4*>(sm + 4 * tid);
+#pragma unroll
+    for (int q = 1; q < 4; ++q) {
+        const float4 w = *reinterpret_cast<const float4*>(sm + q * kPT * kPT + 4 * tid);
+        t.x += w.x, t.y += w.y, t.z += w.z, t.w += w.w;
+    }
+
+    auto store_c = [&](float4 s) {
+        const float sv[4] = {s.x, s.y, s.z, s.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = 4 * tid + q, i = i0 + (e & 31), j = j0 + (e >> 5);
+            if (i < p.n1 && j < p.n2) {
+                float* c = p.C + i + (int64_t)j * p.ldc;
+                *c = p.beta == 0.f ? p.alpha * sv[q] : p.alpha * sv[q] + p.beta * *c;
+            }
+        }
+    };
+    if (p.S == 1) {
+        store_c(t);
+        return;
+    }
+    constexpr int E = kPT * kPT;
+    __stcg(reinterpret_cast<float4*>(p.part + ((int64_t)tile * p.S + chunk) * E) + tid, t);
+    __threadfence();
+    __syncthreads();
+    int* cnt = p.cnt + tile * (p.G + 1);
+    const int grp = chunk / p.g, g0 = grp * p.g, gn = min(p.g, p.S - g0);
+    if (tid == 0) s_last = atomicAdd(cnt + grp, 1) == gn - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    float4 u = sum_partials(reinterpret_cast<const float4*>(p.part + ((int64_t)tile * p.S + g0) * E) + tid, gn);
+    if (p.G > 1) {
+        __stcg(reinterpret_cast<float4*>(p.gpart + ((int64_t)tile * p.G + grp) * E) + tid, u);
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) s_last = atomicAdd(cnt + p.G, 1) == p.G - 1;
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        u = sum_partials(reinterpret_cast<const float4*>(p.gpart + (int64_t)tile * p.G * E) + tid, p.G);
+    }
+    store_c(u);
+    if (tid <= p.G) cnt[tid] = 0;  // every CTA of the tile has counted: ready for the next launch
+}
+
+// ---------------------------------------------------------------------------
+// FP32 update on CUDA cores: A2 (m x n2) += alpha A1 (m x n1) X (n1 x n2,
+// ldx), A1 and A2 sharing lda, n1 <= 256.  A CTA owns a 32-column tile of
+// A2 (blockIdx.y) and walks 128-row blocks (grid-stride, one wave).  X's
+// n1 x 32 tile stays in shared memory for the whole launch.  A block's A1
+// rows are staged 32 columns at a time (a straight copy of the column-major
+// data, 16-byte stores); the next chunk, or the next block's first chunk
+// and its A2 tile, are loaded into registers while the current chunk is
+// multiplied.  Each thread owns 4 rows x 4 columns of the block and reads A1
+// and X as 16-byte shared-memory vectors.
+constexpr int kNR = 128;    // rows per block
+constexpr int kNK = 32;     // K per staged chunk
+constexpr int kNXs = 36;    // row stride of the X tile in shared memory (16-byte rows, 4-way store conflicts)
+constexpr int kNMaxK = 256;
+
+struct NnFusedArgs {
+    int64_t m;
+    int n1, n2;
+    const float* A1;
+    float* A2;
+    int64_t lda;
+    const float* X;
+    int64_t ldx;
+    float alpha;
+};
+
+size_t nn_fused_smem(int n1) { return ((size_t)round_up(n1, kNK) * kNXs + (size_t)kNK * kNR) * sizeof(float); }
+
+template <bool VEC>
+__global__ void __launch_bounds__(256, 2) gemm_nn_fused(NnFusedArgs p) {
+    extern __shared__ __align__(16) float nn_smem[];
+    const int n1p = (p.n1 + kNK - 1) / kNK * kNK;
+    float* Xs = nn_smem;              // [n1p][kNXs]
+    float* As = nn_smem + n1p * kNXs;  // [kNK][kNR]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int j0 = blockIdx.y * 32;
+    for (int e = tid; e < n1p * 32; e += 256) {
+        const int i = e % n1p, j = e / n1p;
+        Xs[i * kNXs + j] = (i < p.n1 && j0 + j < p.n2) ? p.X[i + (int64_t)(j0 + j) * p.ldx] : 0.f;
+    }
+    // compute: rows 4rg..4rg+3, columns 4cg..4cg+3 of the block
+    const int rg = (warp & 3) * 8 + (lane & 7), cg = (warp >> 2) * 4 + (lane >> 3);
+    const int64_t nblk = (p.m + kNR - 1) / kNR;
+
+    // A1 chunk loader: float4 slot e = rows 4(idx%32).., column idx/32 of the chunk
+    float4 ra[4];
+    auto fetch_a = [&](int64_t row0, int kc) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int idx = tid + 256 * e, kk = idx >> 5;
+            const int64_t r = row0 + 4 * (idx & 31);
+            const int k = kc + kk;
+            const float* q = p.A1 + (int64_t)k * p.lda + r;
+            if (k >= p.n1) {
+                ra[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+            } else if (VEC && r + 3 < p.m) {
+                ra[e] = __ldg(reinterpret_cast<const float4*>(q));
+            } else {
+                ra[e].x = r < p.m ? __ldg(q) : 0.f;
+                ra[e].y = r + 1 < p.m ? __ldg(q + 1) : 0.f;
+                ra[e].z = r + 2 < p.m ? __ldg(q + 2) : 0.f;
+                ra[e].w = r + 3 < p.m ? __ldg(q + 3) : 0.f;
+            }
+        }
+    };
+    // A2 tile of the thread: column 4cg + v, rows 4rg..4rg+3
+    float4 rc[4];
+    auto fetch_c = [&](int64_t row0) {
+        const int64_t r = row0 + 4 * rg;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int j = j0 + 4 * cg + v;
+            const float* q = p.A2 + (int64_t)(j < p.n2 ? j : 0) * p.lda + r;
+            if (j >= p.n2) {
+                rc[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+            } else if (VEC && r + 3 < p.m) {
+                rc[v] = *reinterpret_cast<const float4*>(q);
+            } else {
+                rc[v].x = r < p.m ? q[0] : 0.f;
+                rc[v].y = r + 1 < p.m ? q[1] : 0.f;
+                rc[v].z = r + 2 < p.m ? q[2] : 0.f;
+                rc[v].w = r + 3 < p.m ? q[3] : 0.f;
+            }
+        }
+    };
+
+    int64_t blk = blockIdx.x;
+    if (blk < nblk) {
+        fetch_a(blk * kNR, 0);
+        fetch_c(blk * kNR);
+    }
+    for (; blk < nblk; blk += gridDim.x) {
+        const int64_t row0 = blk * kNR;
+        float4 c[4] = {rc[0], rc[1], rc[2], rc[3]};
+        float acc[4][4] = {};
+        for (int kc = 0; kc < p.n1; kc += kNK) {
+            __syncthreads();  // the previous chunk's reads of As are done (and, first, Xs is written)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int idx = tid + 256 * e;
+                *reinterpret_cast<float4*>(As + (idx >> 5) * kNR + 4 * (idx & 31)) = ra[e];
+            }
+            __syncthreads();
+            if (kc + kNK < p.n1) {
+                fetch_a(row0, kc + kNK);
+            } else if (blk + gridDim.x < nblk) {
+                fetch_a((blk + gridDim.x) * kNR, 0);
+                fetch_c((blk + gridDim.x) * kNR);
+            }
+#pragma unroll 8
+            for (int kk = 0; kk < kNK; ++kk) {
+                const float4 a = *reinterpret_cast<const float4*>(As + kk * kNR + 4 * rg);
+                const float4 x = *reinterpret_cast<const float4*>(Xs + (kc + kk) * kNXs + 4 * cg);
+                const float av[4] = {a.x, a.y, a.z, a.w}, xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], xv[v], acc[u][v]);
+            }
+        }
+        const int64_t r = row0 + 4 * rg;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int j = j0 + 4 * cg + v;
+            if (j >= p.n2) continue;
+            float4 o = c[v];
+            o.x = fmaf(p.alpha, acc[0][v], o.x);
+            o.y = fmaf(p.alpha, acc[1][v], o.y);
+            o.z = fmaf(p.alpha, acc[2][v], o.z);
+            o.w = fmaf(p.alpha, acc[3][v], o.w);
+            float* q = p.A2 + (int64_t)j * p.lda + r;
+            if (VEC && r + 3 < p.m) {
+                *reinterpret_cast<float4*>(q) = o;
+            } else {
+                if (r < p.m) q[0] = o.x;
+                if (r + 1 < p.m) q[1] = o.y;
+                if (r + 2 < p.m) q[2] = o.z;
+                if (r + 3 < p.m) q[3] = o.w;
+            }
+        }
     }
 }
 
@@ -204,11 +587,18 @@ GemmPlan tn_plan(int64_t M, int64_t N, int64_t K) {
     return {(int)nz, kchunk};
 }
 
+// Bytes of partial sums proj_tn needs for an n1 x n2 projection over K rows.
+template <typename T>
+size_t proj_tn_part_bytes(int64_t n1, int64_t n2, int64_t K) {
+    if (std::is_same<T, float>::value) return tn_fused_plan(n1, n2, K).part_bytes();
+    return (size_t)tn_plan(n1, n2, K).nz * n1 * n2 * sizeof(T);
+}
+
 // Workspace layout: [status word | tsqr region | partial sums | reorth temp].
 // The precision form (FP32, TF32X3) sizes the TSQR region for the
 // precision-form TSQR and the partial sums for the tcgen05 split-K GEMM.
 struct QrWs {
-    size_t err_bytes = 256, tsqr_bytes = 0, part_bytes = 0, tmp_bytes = 0;
+    size_t err_bytes = kPHeader, tsqr_bytes = 0, part_bytes = 0, tmp_bytes = 0;
     size_t total() const { return err_bytes + tsqr_bytes + part_bytes + tmp_bytes; }
 };
 
@@ -237,8 +627,9 @@ void qr_ws_walk(int64_t m, int64_t n, int nb, bool reorth, bool tc, QrWs* w) {
         return;
     }
     const int64_t n1 = split_of(n, nb), n2 = n - n1;
-    const int64_t nz = tc_projection(tc, n1, n2) ? tc_tn_splits(n1, n2, m) : tn_plan(n1, n2, m).nz;
-    w->part_bytes = std::max(w->part_bytes, (size_t)round_up(nz * n1 * n2 * (int64_t)sizeof(T), 256));
+    const size_t pb = tc_projection(tc, n1, n2) ? (size_t)tc_tn_splits(n1, n2, m) * n1 * n2 * sizeof(T)
+                                                : proj_tn_part_bytes<T>(n1, n2, m);
+    w->part_bytes = std::max(w->part_bytes, (size_t)round_up((int64_t)pb, 256));
     if (reorth) w->tmp_bytes = std::max(w->tmp_bytes, (size_t)round_up(n1 * n2 * (int64_t)sizeof(T), 256));
     qr_ws_walk<T>(m, n1, nb, reorth, tc, w);
     qr_ws_walk<T>(m, n2, nb, reorth, tc, w);
@@ -251,36 +642,119 @@ void proj_tn_tc(int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2, int
     if constexpr (std::is_same<T, float>::value) {
         const int nz = tc_gemm_tn((int)n1, (int)n2, m, A1, lda, A2, lda, P, err, s, bf16);
         log_launch(kTagTc + 100, s);
-        const int64_t total = n1 * n2;
-        int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 1024);
-        reduce_partials<T><<<blocks, 256, 0, s>>>((int)n1, (int)n2, nz, P, T(1), beta, C, ldc);
+        reduce_partials<T><<<reduce_blocks(n1 * n2), 256, 0, s>>>((int)n1, (int)n2, nz, P, T(1), beta, C, ldc);
         log_launch(kTagReduce, s);
     }
 }
 
-// A2 (m x n2) -= A1 (m x n1) X (n1 x n2) on the tensor cores (FP32 only).
+// A2 (m x n2) -= A1 (m x n1) X (n1 x n2, ldx) in FP32 on CUDA cores
+// (gemm_nn_fused, n1 <= 256).
+void update_nn_fused(int64_t m, int64_t n1, int64_t n2, const float* A1, int64_t lda, const float* X, int64_t ldx,
+                     float* A2, cudaStream_t s) {
+    NnFusedArgs a;
+    a.m = m;
+    a.n1 = (int)n1;
+    a.n2 = (int)n2;
+    a.A1 = A1;
+    a.A2 = A2;
+    a.lda = lda;
+    a.X = X;
+    a.ldx = ldx;
+    a.alpha = -1.f;
+    const int tj = (int)ceil_div(n2, 32);
+    const int64_t resident = 2 * (int64_t)device_sm_count();
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(m, kNR), ceil_div(resident, tj)));
+    const size_t smem = nn_fused_smem((int)n1);
+    static PerDeviceOnce attr;
+    attr.run([] {
+        const int mx = (int)nn_fused_smem(kNMaxK);
+        cudaFuncSetAttribute(gemm_nn_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(gemm_nn_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    });
+    const bool vec = lda % 4 == 0 && reinterpret_cast<uintptr_t>(A1) % 16 == 0 &&
+                     reinterpret_cast<uintptr_t>(A2) % 16 == 0;
+    if (vec)
+        gemm_nn_fused<true><<<dim3((unsigned)gx, (unsigned)tj), 256, smem, s>>>(a);
+    else
+        gemm_nn_fused<false><<<dim3((unsigned)gx, (unsigned)tj), 256, smem, s>>>(a);
+    log_launch(kTagGemmNN, s);
+}
+
+// The tensor-core forms' updates run on the tcgen05 GEMM only when the
+// panel is wider than kNnTcMin.  Measured at 131,072 x 512 (TF32x3,
+// reorthogonalised): 6.156 ms with the CUDA-core kernel up to 64 columns,
+// 5.966 ms up to 128, 6.077 ms up to 256.
+constexpr int64_t kNnTcMin = 128;
+
+// A2 (m x n2) -= A1 (m x n1) X (n1 x n2) in a tensor-core form (FP32 only).
 template <typename T>
 void update_nn_tc(int64_t m, int64_t n1, int64_t n2, const T* A1, int64_t lda, const T* X, int64_t ldx, T* A2,
                   int* err, cudaStream_t s, bool bf16) {
     if constexpr (std::is_same<T, float>::value) {
+        if (n1 <= kNnTcMin) return update_nn_fused(m, n1, n2, A1, lda, X, ldx, A2, s);
         tc_gemm_nn(m, (int)n2, (int)n1, -1.f, A1, lda, X, ldx, A2, lda, err, s, bf16);
         log_launch(kTagTc + 101, s);
     }
 }
 
+// A2 (m x n2) -= A1 (m x n1) X (n1 x n2, ldx) on CUDA cores, plain form.
+template <typename T>
+void update_nn(int64_t m, int64_t n1, int64_t n2, const T* A1, int64_t lda, const T* X, int64_t ldx, T* A2,
+               cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (n1 <= kNMaxK) return update_nn_fused(m, n1, n2, A1, lda, X, ldx, A2, s);
+    }
+    dim3 g((unsigned)ceil_div(m, kTile), (unsigned)ceil_div(n2, kTile));
+    gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, X, ldx, T(1), A2, lda);
+    log_launch(kTagGemmNN, s);
+}
+
+// C (n1 x n2, ldc) = A1^T A2 (+ beta C) on CUDA cores.  FP32: one launch of
+// gemm_tn_fused (cnt: the workspace's counter words, zero between
+// launches); FP64: split-K partials, then their sum.
 template <typename T>
 tsqr_status proj_tn(int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2, int64_t lda, T* P, T* C,
-                    int64_t ldc, T beta, cudaStream_t s) {
+                    int64_t ldc, T beta, int* cnt, cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        const TnFusedPlan fp = tn_fused_plan(n1, n2, m);
+        TnFusedArgs a;
+        a.n1 = (int)n1;
+        a.n2 = (int)n2;
+        a.K = m;
+        a.A = A1;
+        a.B = A2;
+        a.ld = lda;
+        a.C = C;
+        a.ldc = ldc;
+        a.alpha = 1.f;
+        a.beta = beta;
+        a.tiles_i = fp.tiles_i;
+        a.S = fp.S;
+        a.g = fp.g;
+        a.G = fp.G;
+        a.kchunk = fp.kchunk;
+        a.part = P;
+        a.gpart = P + (size_t)fp.ntiles * fp.S * kPT * kPT;
+        a.cnt = cnt;
+        const dim3 g((unsigned)fp.ntiles, (unsigned)fp.S);
+        const bool vec = lda % 4 == 0 && reinterpret_cast<uintptr_t>(A1) % 16 == 0 &&
+                         reinterpret_cast<uintptr_t>(A2) % 16 == 0;
+        if (vec)
+            gemm_tn_fused<true><<<g, 256, 0, s>>>(a);
+        else
+            gemm_tn_fused<false><<<g, 256, 0, s>>>(a);
+        log_launch(kTagGemmTN, s);
+        return TSQR_OK;
+    }
     GemmPlan gp = tn_plan(n1, n2, m);
     dim3 g((unsigned)ceil_div(n1, kTile), (unsigned)ceil_div(n2, kTile), (unsigned)gp.nz);
     gemm_tn_partial<T><<<g, 256, 0, s>>>((int)n1, (int)n2, m, A1, lda, A2, lda, P, gp.kchunk);
     log_launch(kTagGemmTN, s);
-    const int64_t total = n1 * n2;
-    int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 1024);
-    reduce_partials<T><<<blocks, 256, 0, s>>>((int)n1, (int)n2, gp.nz, P, T(1), beta, C, ldc);
+    reduce_partials<T><<<reduce_blocks(n1 * n2), 256, 0, s>>>((int)n1, (int)n2, gp.nz, P, T(1), beta, C, ldc);
     log_launch(kTagReduce, s);
     return TSQR_OK;
 }
+
 
 template <typename T>
 tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, char* ws, const QrWs& w,
@@ -301,34 +775,32 @@ tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, c
     T* R12 = R + n1 * ldr;
     T* R22 = R + n1 * ldr + n1;
     int* err = reinterpret_cast<int*>(ws);
+    int* cnt = err + kPCounters;
     T* P = reinterpret_cast<T*>(tws + w.tsqr_bytes);
     T* tmp = reinterpret_cast<T*>(tws + w.tsqr_bytes + w.part_bytes);
     tsqr_status st = qr_rec<T>(m, n1, A1, lda, R11, ldr, ws, w, o, s);
     if (st != TSQR_OK) return st;
-    dim3 g((unsigned)ceil_div(m, kTile), (unsigned)ceil_div(n2, kTile));
     const bool tcp = tc_projection(tc, n1, n2);
     if (tc) {
         if (tcp)
             proj_tn_tc<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), err, s, use_bf16<T>(o));
         else
-            proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), s);
+            proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), cnt, s);
         update_nn_tc<T>(m, n1, n2, A1, lda, R12, ldr, A2, err, s, use_bf16<T>(o));
     } else {
-        proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), s);
-        gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, R12, ldr, T(1), A2, lda);
-        log_launch(kTagGemmNN, s);
+        proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), cnt, s);
+        update_nn<T>(m, n1, n2, A1, lda, R12, ldr, A2, s);
     }
     if (o.reorth) {
         if (tc) {
             if (tcp)
                 proj_tn_tc<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), err, s, use_bf16<T>(o));
             else
-                proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), s);
+                proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), cnt, s);
             update_nn_tc<T>(m, n1, n2, A1, lda, tmp, n1, A2, err, s, use_bf16<T>(o));
         } else {
-            proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), s);
-            gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, tmp, n1, T(1), A2, lda);
-            log_launch(kTagGemmNN, s);
+            proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), cnt, s);
+            update_nn<T>(m, n1, n2, A1, lda, tmp, n1, A2, s);
         }
         int blocks = (int)std::min<int64_t>(ceil_div(n1 * n2, 256), 1024);
         axpy_block<T><<<blocks, 256, 0, s>>>((int)n1, (int)n2, tmp, n1, R12, ldr);
@@ -511,7 +983,7 @@ __global__ void __launch_bounds__(256) panel_q_rows(int64_t rows, int bw, T* Y, 
 // Workspace: [status word | leaf TSQR | split-K partials | Rp, U^-1, M of a
 // leaf | W, X (n1 x n2 each) | T of the whole matrix (n x n)].
 struct HqrWs {
-    size_t err = 256, tsqr = 0, part = 0, small = 0, wx = 0, tfull = 0;
+    size_t err = kPHeader, tsqr = 0, part = 0, small = 0, wx = 0, tfull = 0;
     size_t total() const { return err + tsqr + part + small + wx + tfull; }
 };
 
@@ -524,8 +996,9 @@ void hqr_ws_walk(int64_t m, int64_t n, int b, bool tc, HqrWs* w) {
     }
     const int64_t n1 = split_of(n, b), n2 = n - n1;
     for (int64_t K : {m, m - n1}) {
-        const int64_t nz = tc_projection(tc, n1, n2) ? tc_tn_splits(n1, n2, K) : tn_plan(n1, n2, K).nz;
-        w->part = std::max(w->part, (size_t)round_up(nz * n1 * n2 * (int64_t)sizeof(T), 256));
+        const size_t pb = tc_projection(tc, n1, n2) ? (size_t)tc_tn_splits(n1, n2, K) * n1 * n2 * sizeof(T)
+                                                    : proj_tn_part_bytes<T>(n1, n2, K);
+        w->part = std::max(w->part, (size_t)round_up((int64_t)pb, 256));
     }
     w->wx = std::max(w->wx, 2 * (size_t)round_up(n1 * n2 * (int64_t)sizeof(T), 256));
     hqr_ws_walk<T>(m, n1, b, tc, w);
@@ -564,7 +1037,7 @@ void hqr_tn(const HqrCtx<T>& c, int64_t m, int64_t n1, int64_t n2, const T* A1, 
     if (tc_projection(c.tc, n1, n2))
         proj_tn_tc<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.err, c.s, c.bf16);
     else
-        proj_tn<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.s);
+        proj_tn<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.err + kPCounters, c.s);
 }
 
 // A2 (m x n2) -= Y (m x n1) X (n1 x n2, ld n1)
@@ -573,9 +1046,7 @@ void hqr_nn(const HqrCtx<T>& c, int64_t m, int64_t n1, int64_t n2, const T* Y, c
     if (c.tc) {
         update_nn_tc<T>(m, n1, n2, Y, c.lda, X, n1, A2, c.err, c.s, c.bf16);
     } else {
-        dim3 g((unsigned)ceil_div(m, kTile), (unsigned)ceil_div(n2, kTile));
-        gemm_nn<T><<<g, 256, 0, c.s>>>(m, (int)n2, (int)n1, T(-1), Y, c.lda, X, n1, T(1), A2, c.lda);
-        log_launch(kTagGemmNN, c.s);
+        update_nn<T>(m, n1, n2, Y, c.lda, X, n1, A2, c.s);
     }
 }
 
@@ -680,7 +1151,8 @@ tsqr_status hqr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, 
     c.bf16 = use_bf16<T>(o);
     c.b = b;
     c.s = s;
-    if (tc && cudaMemsetAsync(c.err, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
+    // status word and the projection's counters
+    if (cudaMemsetAsync(c.err, 0, kPHeader, s) != cudaSuccess) return TSQR_ERR_CUDA;
     if (cudaMemset2DAsync(R, ldr * sizeof(T), 0, n * sizeof(T), n, s) != cudaSuccess) return TSQR_ERR_CUDA;
     if (cudaMemsetAsync(Tfull, 0, n * n * sizeof(T), s) != cudaSuccess) return TSQR_ERR_CUDA;
     tsqr_status st = hqr_factor<T>(c, m, n, A, R, Tfull);
@@ -706,7 +1178,8 @@ tsqr_status qr_run(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, v
     QrWs w;
     qr_ws_walk<T>(m, n, panel_of(o), o.reorth != 0, use_tc<T>(o), &w);
     if (work == nullptr || work_bytes < w.total()) return TSQR_ERR_WORKSPACE;
-    if (use_tc<T>(o) && cudaMemsetAsync(work, 0, sizeof(int), s) != cudaSuccess) return TSQR_ERR_CUDA;
+    // status word and the projection's counters
+    if (cudaMemsetAsync(work, 0, kPHeader, s) != cudaSuccess) return TSQR_ERR_CUDA;
     return qr_rec<T>(m, n, A, lda, R, ldr, reinterpret_cast<char*>(work), w, o, s);
 }
 
