@@ -316,7 +316,29 @@ def run_e2e(tg, A0, form, steps, warmup, device):
     # the host results are the product of the last step: check them
     Qd, Rd = hQ.to(device), hR.to(device)
     back, orth = check_errors(A0, Qd, Rd)
-    return {"ms": ms, "h2d": m * n * 4, "d2h": m * n * 4 + n * n * 4, "backward": back, "orth": orth}
+    # The host link alone: a plain copy of A in and of Q out, each timed
+    # alone (best of 3).  Q's copy-back needs the whole up-sweep, so a call
+    # cannot overlap the two directions: their sum bounds the call.
+    dA = torch.empty_like(Qd)
+
+    def best(fn):
+        t = []
+        for _ in range(3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            t.append(a.elapsed_time(b))
+        return min(t)
+
+    h2d_ms = best(lambda: dA.copy_(hA, non_blocking=True))
+    d2h_ms = best(lambda: hQ.copy_(dA, non_blocking=True))
+    nbytes = m * n * 4
+    link = {"h2d_gbs": nbytes / (h2d_ms * 1e-3) / 1e9, "d2h_gbs": nbytes / (d2h_ms * 1e-3) / 1e9,
+            "bound_ms": h2d_ms + d2h_ms, "frac_of_bound": (h2d_ms + d2h_ms) / ms}
+    return {"ms": ms, "h2d": m * n * 4, "d2h": m * n * 4 + n * n * 4, "backward": back, "orth": orth,
+            "host_link": link}
 
 
 def run_implicit(tg, A0, steps, warmup, device, flush):
@@ -943,7 +965,7 @@ def main():
         "e2e": {"value": e2e_val, "unit": "TFLOP/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"], "ms_per_step": e2e["ms"],
                 "api": "tsqr_s_host (pinned host A in, Q and R out; copies pipelined with the level-0 kernels)",
-                "backward": e2e["backward"], "orth": e2e["orth"]},
+                "backward": e2e["backward"], "orth": e2e["orth"], "host_link": e2e["host_link"]},
         "implicit_q": implicit, "reference_protocol": ref_protocol, "suite": suite,
         "cpu_baseline": cpu, "cpu_lapack": lap,
         "clocks": clocks, "gpu_launches": nl * args.steps, "launches_per_step": nl,

@@ -101,6 +101,6 @@ def test_no_new_or_larger_spills(spills):
 @pytest.mark.parametrize("kernel", ["tsqr::factor_split_tiles<float, 32, 4, 16, 2, false>",
                                     "tsqr::factor_split_tiles<float, 16, 4, 16, 4, false>",
                                     "tsqr::apply_tiles<float, 32, 256, 2, 2>",
-                                    "tsqr::tc_apply_tiles<32, 512>"])
+                                    "tsqr::tc_apply_tiles<32, 512, true>"])
 def test_headline_kernels_do_not_spill(spills, kernel):
     assert kernel not in spills

@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "tc.cuh"
 
 namespace tsqr {
 
@@ -192,6 +193,8 @@ struct TnFusedArgs {
     float* part;  // [ntiles][S][1024]
     float* gpart;  // [ntiles][G][1024]
     int* cnt;      // [ntiles][G + 1], zero between launches
+    int* err;      // status word (TMA form: a bounded wait gave up)
+    int tries;     // polls of a bounded wait
 };
 
 // sum over z < n of q[z * 256] (float4 elements), in order of z, read from
@@ -209,6 +212,160 @@ __device__ __forceinline__ float4 sum_partials(const float4* q, int n) {
         for (int e = 0; e < 8; ++e) u.x += w[e].x, u.y += w[e].y, u.z += w[e].z, u.w += w[e].w;
     }
     return u;
+}
+
+// The CTA's partial tile t (elements 4 tid .. 4 tid + 3 of the column-major
+// 32 x 32 tile, in every thread) into C: directly when the tile has one
+// chunk, else through the chunk partials and the two last-arriver sums.
+__device__ __forceinline__ void tn_finish(const TnFusedArgs& p, float4 t, int tile, int chunk, int i0, int j0,
+                                          int& s_last) {
+    const int tid = threadIdx.x;
+    auto store_c = [&](float4 s) {
+        const float sv[4] = {s.x, s.y, s.z, s.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = 4 * tid + q, i = i0 + (e & 31), j = j0 + (e >> 5);
+            if (i < p.n1 && j < p.n2) {
+                float* c = p.C + i + (int64_t)j * p.ldc;
+                *c = p.beta == 0.f ? p.alpha * sv[q] : p.alpha * sv[q] + p.beta * *c;
+            }
+        }
+    };
+    if (p.S == 1) {
+        store_c(t);
+        return;
+    }
+    constexpr int E = kPT * kPT;
+    __stcg(reinterpret_cast<float4*>(p.part + ((int64_t)tile * p.S + chunk) * E) + tid, t);
+    __threadfence();
+    __syncthreads();
+    int* cnt = p.cnt + tile * (p.G + 1);
+    const int grp = chunk / p.g, g0 = grp * p.g, gn = min(p.g, p.S - g0);
+    if (tid == 0) s_last = atomicAdd(cnt + grp, 1) == gn - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    float4 u = sum_partials(reinterpret_cast<const float4*>(p.part + ((int64_t)tile * p.S + g0) * E) + tid, gn);
+    if (p.G > 1) {
+        __stcg(reinterpret_cast<float4*>(p.gpart + ((int64_t)tile * p.G + grp) * E) + tid, u);
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) s_last = atomicAdd(cnt + p.G, 1) == p.G - 1;
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        u = sum_partials(reinterpret_cast<const float4*>(p.gpart + (int64_t)tile * p.G * E) + tid, p.G);
+    }
+    store_c(u);
+    if (tid <= p.G) cnt[tid] = 0;  // every CTA of the tile has counted: ready for the next launch
+}
+
+// TMA-fed form (A and B 16-byte aligned, lda a multiple of 4 floats): each
+// 64-row step arrives as four 32 x 32 boxes (A rows 0-31 and 32-63, then B)
+// with the 128-byte swizzle, in a ring of kPStages steps on mbarriers (the
+// copies of the next three steps run under the current step's FMAs).
+// Column c of a box holds 32 rows as 8 chunks of 16 bytes, chunk q at
+// q ^ (c % 8).  Thread (ig, jg) of a K slice owns output rows ig + 8u and
+// columns jg + 8v (u, v < 4): its eight 16-byte reads per 4 rows are free
+// of bank conflicts.  Rows past the matrix end and columns past n1 / n2
+// arrive as zeros; chunks are whole 64-row steps, so a CTA's last step never
+// reaches into the next chunk.  The waits are bounded: after p.tries polls
+// the CTA sets the status word, lets its copies in flight land and stops.
+constexpr int kPStages = 4;
+constexpr int kPBox = kPT * kPT * 4;                       // one 32 x 32 FP32 box
+constexpr int kPStageBytes = 4 * kPBox;                    // A and B, 64 rows each
+constexpr size_t kPTmaSmem = kPStages * kPStageBytes + 1024;  // + alignment of the swizzled boxes
+
+__global__ void __launch_bounds__(256, 3)
+    gemm_tn_tma(TnFusedArgs p, const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb) {
+    extern __shared__ unsigned char tn_raw[];
+    __shared__ unsigned long long mbar[kPStages];
+    __shared__ int s_last;
+    unsigned char* base = tn_raw + ((1024 - (tc::smem_u32(tn_raw) & 1023)) & 1023);
+    const uint32_t sbase = tc::smem_u32(base);
+    const int tid = threadIdx.x;
+    const int tile = blockIdx.x, chunk = blockIdx.y;
+    const int i0 = (tile % p.tiles_i) * kPT, j0 = (tile / p.tiles_i) * kPT;
+    const int64_t kbeg = (int64_t)chunk * p.kchunk;
+    const int64_t kend = min(p.K, kbeg + p.kchunk);
+    const int nst = (int)((kend - kbeg + kPRows - 1) / kPRows);
+    if (tid == 0) {
+        for (int b = 0; b < kPStages; ++b) tc::mbar_init(tc::smem_u32(&mbar[b]), 1);
+        tc::fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int s) {  // thread 0
+        const int b = s % kPStages;
+        const uint32_t dst = sbase + b * kPStageBytes, mb = tc::smem_u32(&mbar[b]);
+        const int x = (int)(kbeg + (int64_t)s * kPRows);
+        tc::fence_smem_to_async();
+        tc::mbar_arrive_expect_tx(mb, kPStageBytes);
+        tc::tma_load_2d(dst, &ta, x, i0, mb);
+        tc::tma_load_2d(dst + kPBox, &ta, x + 32, i0, mb);
+        tc::tma_load_2d(dst + 2 * kPBox, &tb, x, j0, mb);
+        tc::tma_load_2d(dst + 3 * kPBox, &tb, x + 32, j0, mb);
+    };
+    if (tid == 0)
+        for (int s = 0; s < min(kPStages, nst); ++s) issue(s);
+
+    const int sl = tid >> 6, lt = tid & 63, ig = lt & 7, jg = lt >> 3;
+    float acc[4][4] = {};
+    for (int s = 0; s < nst; ++s) {
+        const int b = s % kPStages;
+        const bool ok = tc::mbar_wait(tc::smem_u32(&mbar[b]), (uint32_t)(s / kPStages) & 1u, p.tries);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                if (p.err) atomicExch(p.err, 1);
+                // the steps issued and not consumed: s .. s + kPStages - 1
+                for (int q = s; q < min(s + kPStages, nst); ++q)
+                    (void)tc::mbar_wait(tc::smem_u32(&mbar[q % kPStages]), (uint32_t)(q / kPStages) & 1u);
+            }
+            return;
+        }
+        // slice sl: rows 16 sl .. 16 sl + 15 of the step = box half sl / 2,
+        // 4-row groups (sl % 2) * 4 .. + 3 of it
+        const unsigned char* Ab = base + b * kPStageBytes + (sl >> 1) * kPBox;
+        const unsigned char* Bb = Ab + 2 * kPBox;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int k4 = (sl & 1) * 4 + q;
+            float4 a[4], bv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                a[u] = *reinterpret_cast<const float4*>(Ab + (ig + 8 * u) * 128 + ((k4 ^ ig) << 4));
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+                bv[v] = *reinterpret_cast<const float4*>(Bb + (jg + 8 * v) * 128 + ((k4 ^ jg) << 4));
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    float c = acc[u][v];
+                    c = fmaf(a[u].x, bv[v].x, c);
+                    c = fmaf(a[u].y, bv[v].y, c);
+                    c = fmaf(a[u].z, bv[v].z, c);
+                    c = fmaf(a[u].w, bv[v].w, c);
+                    acc[u][v] = c;
+                }
+        }
+        __syncthreads();  // every thread is done with buffer b
+        if (tid == 0 && s + kPStages < nst) issue(s + kPStages);
+    }
+    // the four slices' tiles (column-major, element j * 32 + i) in the ring's
+    // first 16 KB: every copy has landed, all were waited for above
+    float* red = reinterpret_cast<float*>(base);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) red[sl * kPT * kPT + (jg + 8 * v) * kPT + ig + 8 * u] = acc[u][v];
+    __syncthreads();
+    float4 t = *reinterpret_cast<const float4*>(red + 4 * tid);
+#pragma unroll
+    for (int q = 1; q < 4; ++q) {
+        const float4 w = *reinterpret_cast<const float4*>(red + q * kPT * kPT + 4 * tid);
+        t.x += w.x, t.y += w.y, t.z += w.z, t.w += w.w;
+    }
+    tn_finish(p, t, tile, chunk, i0, j0, s_last);
 }
 
 template <bool VEC>
@@ -304,45 +461,7 @@ __global__ void __launch_bounds__(256, 3) gemm_tn_fused(TnFusedArgs p) {
         const float4 w = *reinterpret_cast<const float4*>(sm + q * kPT * kPT + 4 * tid);
         t.x += w.x, t.y += w.y, t.z += w.z, t.w += w.w;
     }
-
-    auto store_c = [&](float4 s) {
-        const float sv[4] = {s.x, s.y, s.z, s.w};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = 4 * tid + q, i = i0 + (e & 31), j = j0 + (e >> 5);
-            if (i < p.n1 && j < p.n2) {
-                float* c = p.C + i + (int64_t)j * p.ldc;
-                *c = p.beta == 0.f ? p.alpha * sv[q] : p.alpha * sv[q] + p.beta * *c;
-            }
-        }
-    };
-    if (p.S == 1) {
-        store_c(t);
-        return;
-    }
-    constexpr int E = kPT * kPT;
-    __stcg(reinterpret_cast<float4*>(p.part + ((int64_t)tile * p.S + chunk) * E) + tid, t);
-    __threadfence();
-    __syncthreads();
-    int* cnt = p.cnt + tile * (p.G + 1);
-    const int grp = chunk / p.g, g0 = grp * p.g, gn = min(p.g, p.S - g0);
-    if (tid == 0) s_last = atomicAdd(cnt + grp, 1) == gn - 1;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    float4 u = sum_partials(reinterpret_cast<const float4*>(p.part + ((int64_t)tile * p.S + g0) * E) + tid, gn);
-    if (p.G > 1) {
-        __stcg(reinterpret_cast<float4*>(p.gpart + ((int64_t)tile * p.G + grp) * E) + tid, u);
-        __threadfence();
-        __syncthreads();
-        if (tid == 0) s_last = atomicAdd(cnt + p.G, 1) == p.G - 1;
-        __syncthreads();
-        if (!s_last) return;
-        __threadfence();
-        u = sum_partials(reinterpret_cast<const float4*>(p.gpart + (int64_t)tile * p.G * E) + tid, p.G);
-    }
-    store_c(u);
-    if (tid <= p.G) cnt[tid] = 0;  // every CTA of the tile has counted: ready for the next launch
+    tn_finish(p, t, tile, chunk, i0, j0, s_last);
 }
 
 // ---------------------------------------------------------------------------
@@ -714,7 +833,7 @@ void update_nn(int64_t m, int64_t n1, int64_t n2, const T* A1, int64_t lda, cons
 // launches); FP64: split-K partials, then their sum.
 template <typename T>
 tsqr_status proj_tn(int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2, int64_t lda, T* P, T* C,
-                    int64_t ldc, T beta, int* cnt, cudaStream_t s) {
+                    int64_t ldc, T beta, int* cnt, int* err, cudaStream_t s) {
     if constexpr (std::is_same<T, float>::value) {
         const TnFusedPlan fp = tn_fused_plan(n1, n2, m);
         TnFusedArgs a;
@@ -736,7 +855,20 @@ tsqr_status proj_tn(int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2,
         a.part = P;
         a.gpart = P + (size_t)fp.ntiles * fp.S * kPT * kPT;
         a.cnt = cnt;
+        a.err = err;
+        a.tries = wait_tries().load(std::memory_order_relaxed);
         const dim3 g((unsigned)fp.ntiles, (unsigned)fp.S);
+        CUtensorMap ta, tb;
+        if (m + kPRows <= INT32_MAX && tensor_map_f32(&ta, A1, lda, m, n1, 32, 32, true) &&
+            tensor_map_f32(&tb, A2, lda, m, n2, 32, 32, true)) {
+            static PerDeviceOnce attr;
+            attr.run([] {
+                cudaFuncSetAttribute(gemm_tn_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPTmaSmem);
+            });
+            gemm_tn_tma<<<g, 256, kPTmaSmem, s>>>(a, ta, tb);
+            log_launch(kTagGemmTN, s);
+            return TSQR_OK;
+        }
         const bool vec = lda % 4 == 0 && reinterpret_cast<uintptr_t>(A1) % 16 == 0 &&
                          reinterpret_cast<uintptr_t>(A2) % 16 == 0;
         if (vec)
@@ -785,10 +917,10 @@ tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, c
         if (tcp)
             proj_tn_tc<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), err, s, use_bf16<T>(o));
         else
-            proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), cnt, s);
+            proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), cnt, err, s);
         update_nn_tc<T>(m, n1, n2, A1, lda, R12, ldr, A2, err, s, use_bf16<T>(o));
     } else {
-        proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), cnt, s);
+        proj_tn<T>(m, n1, n2, A1, A2, lda, P, R12, ldr, T(0), cnt, err, s);
         update_nn<T>(m, n1, n2, A1, lda, R12, ldr, A2, s);
     }
     if (o.reorth) {
@@ -796,10 +928,10 @@ tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, c
             if (tcp)
                 proj_tn_tc<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), err, s, use_bf16<T>(o));
             else
-                proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), cnt, s);
+                proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), cnt, err, s);
             update_nn_tc<T>(m, n1, n2, A1, lda, tmp, n1, A2, err, s, use_bf16<T>(o));
         } else {
-            proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), cnt, s);
+            proj_tn<T>(m, n1, n2, A1, A2, lda, P, tmp, n1, T(0), cnt, err, s);
             update_nn<T>(m, n1, n2, A1, lda, tmp, n1, A2, s);
         }
         int blocks = (int)std::min<int64_t>(ceil_div(n1 * n2, 256), 1024);
@@ -1037,7 +1169,7 @@ void hqr_tn(const HqrCtx<T>& c, int64_t m, int64_t n1, int64_t n2, const T* A1, 
     if (tc_projection(c.tc, n1, n2))
         proj_tn_tc<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.err, c.s, c.bf16);
     else
-        proj_tn<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.err + kPCounters, c.s);
+        proj_tn<T>(m, n1, n2, A1, A2, c.lda, c.part, C, n1, T(0), c.err + kPCounters, c.err, c.s);
 }
 
 // A2 (m x n2) -= Y (m x n1) X (n1 x n2, ld n1)

@@ -1,5 +1,6 @@
 // internal.h -- declarations shared by the library's translation units.
 #pragma once
+#include <cuda.h>  // CUtensorMap (the type only; the encoder is looked up at run time)
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -45,6 +46,16 @@ class PerDeviceOnce {
     std::atomic<uint64_t> done_{0};
     std::mutex mu_;
 };
+
+// TMA tensor map of a column-major FP32 matrix (rows x cols, leading
+// dimension ld) for boxes of box_rows x box_cols; rows and columns past the
+// ends read as zeros.  swizzle128: the 128-byte swizzle (box_rows * 4 must
+// then be 128; the destination must be 1024-byte aligned), where the 16-byte
+// chunk q of the box's column c lands at chunk q ^ (c % 8).  False when the
+// matrix does not meet TMA's rules (16-byte base, ld a multiple of 4 floats)
+// or the driver offers no encoder (tsqr.cu).
+bool tensor_map_f32(CUtensorMap* map, const float* base, int64_t ld, int64_t rows, int64_t cols, int box_rows,
+                    int box_cols, bool swizzle128);
 
 // Streaming multiprocessors of the current device, cached per device (148
 // if the attribute cannot be read; the launch that follows then reports the

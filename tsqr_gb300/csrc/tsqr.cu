@@ -42,20 +42,27 @@ EncodeTiledFn encode_tiled() {
     return fn;
 }
 
-// Tensor map of an FP32 level matrix (h rows x n columns, leading dimension
-// ld) for boxes of 256 rows x nbox columns; rows >= h and columns >= n read
-// as zeros.  False when the matrix does not meet TMA's rules (16-byte base,
-// ld a multiple of 4 floats).
-bool level_tensor_map(CUtensorMap* map, const float* M, int64_t ld, int64_t h, int n, int nbox) {
+}  // namespace
+
+bool tensor_map_f32(CUtensorMap* map, const float* base, int64_t ld, int64_t rows, int64_t cols, int box_rows,
+                    int box_cols, bool swizzle128) {
     EncodeTiledFn enc = encode_tiled();
-    if (!enc || (reinterpret_cast<uintptr_t>(M) % 16) != 0 || ld % 4 != 0 || h < 1) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)h, (cuuint64_t)n};
+    if (!enc || (reinterpret_cast<uintptr_t>(base) % 16) != 0 || ld % 4 != 0 || rows < 1 || cols < 1) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)rows, (cuuint64_t)cols};
     const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
-    const cuuint32_t box[2] = {256u, (cuuint32_t)nbox};
+    const cuuint32_t box[2] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols};
     const cuuint32_t estr[2] = {1u, 1u};
-    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(M), dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+namespace {
+
+// Tensor map of an FP32 level matrix (h rows x n columns) for boxes of 256
+// rows x nbox columns.
+bool level_tensor_map(CUtensorMap* map, const float* M, int64_t ld, int64_t h, int n, int nbox) {
+    return tensor_map_f32(map, M, ld, h, n, 256, nbox, false);
 }
 
 template <typename T, int NMAX, int NT, int RPT, int MINB, int AMINB, int ANT = NT, bool NORM64 = false>
