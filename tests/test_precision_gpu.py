@@ -49,9 +49,10 @@ def test_precision_form_matches_oracle(orc, cuda, tg, m, n):
     assert np.abs(Qs - Qt).max() <= 1e-5
 
 
+@pytest.mark.parametrize("n", [32, 64])
 @pytest.mark.parametrize("kappa", [1e3, 1e6])
-def test_precision_form_ill_conditioned(orc, cuda, tg, kappa):
-    A = geometric_matrix(200000, 32, kappa, 8)
+def test_precision_form_ill_conditioned(orc, cuda, tg, kappa, n):
+    A = geometric_matrix(200000, n, kappa, 8)
     dA = to_dev(tg, A)
     dR = tg.tsqr_(dA, precision="tf32x3")
     met = orc.metrics(A, to_host(dA), to_host(dR))

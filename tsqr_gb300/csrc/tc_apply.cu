@@ -52,13 +52,25 @@ struct TcApplySmem {
     uint32_t tmem_slot;
 };
 
-// NF: n == NMAX (no column tests).
+// NF: n == NMAX (no column tests).  Threads: 128 for NMAX <= 32 (4 CTAs
+// per SM); 256 for NMAX = 64 (one CTA per SM, whose shared memory is
+// 130 KB): there thread t owns row t % 128 of each block and columns
+// 32 (t / 128) .. +31, so its rows, prefetch and TMEM read stay at 32
+// values; warp w reads TMEM lanes 32 (w % 4) .. +31 of its column half.
+template <int NMAX>
+constexpr int tc_apply_threads() {
+    return NMAX <= 32 ? 128 : 256;
+}
 template <int NMAX, int B, bool NF>
-__global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyParams<float> p, int* err, int tries) {
-    static_assert(NMAX % 16 == 0 && NMAX <= 256 && B % 128 == 0, "bad shape");
+__global__ void __launch_bounds__(tc_apply_threads<NMAX>(), NMAX <= 32 ? 4 : 1)
+    tc_apply_tiles(ApplyParams<float> p, int* err, int tries) {
+    static_assert(NMAX % 16 == 0 && NMAX <= 64 && B % 128 == 0, "bad shape");
+    constexpr int NT = tc_apply_threads<NMAX>();
+    constexpr int HC = NMAX * 128 / NT;  // columns a thread owns in the block phase
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     TcApplySmem<NMAX>& S = *reinterpret_cast<TcApplySmem<NMAX>*>(tc_smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int rb = tid & 127, cb = (tid >> 7) * HC;  // row in the block, first column
     const int n = p.n;
     constexpr uint32_t kCols = NMAX < 32 ? 32 : NMAX;  // TMEM columns: power of 2 >= 32
     constexpr uint32_t idesc = tc::idesc_tf32(128, NMAX);
@@ -77,19 +89,20 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
     uint32_t phase = 0;
     bool ok = true;
 
-    // Row `blk*128 + tid` of tile tt into v (zero past the tile; the top
+    // Row `blk*128 + rb`, columns cb.., of tile tt into v (zero past the tile; the top
     // n rows come masked from Vt instead).  Issued one block ahead, and for
     // the first block of the next tile before this tile's W products, so
     // the global loads are in flight while the CTA computes.
-    float vnext[NMAX];
-    auto load_block = [&](int64_t tt, int blk, float(&v)[NMAX]) {
+    float vnext[HC];
+    auto load_block = [&](int64_t tt, int blk, float(&v)[HC]) {
         const int64_t r0 = tt * B;
         const int htt = (int)((p.h - r0) < B ? (p.h - r0) : B);
         const float* tl = p.M + r0;
-        const int r = blk * 128 + tid;
+        const int r = blk * 128 + rb;
         const bool rok = r >= n && r < htt;  // the top n rows come from Vt
 #pragma unroll
-        for (int k = 0; k < NMAX; ++k) v[k] = (rok && (NF || k < n)) ? tl[r + (int64_t)k * p.ld] : 0.f;
+        for (int j = 0; j < HC; ++j)
+            v[j] = (rok && (NF || cb + j < n)) ? tl[r + (int64_t)(cb + j) * p.ld] : 0.f;
     };
     if (blockIdx.x < p.ntiles) load_block(blockIdx.x, 0, vnext);
 
@@ -102,11 +115,11 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
         {
             // all global reads first: interleaved with the shared stores they
             // would be issued one at a time (the generic pointers may alias)
-            constexpr int PER = NMAX * NMAX / 128;
+            constexpr int PER = NMAX * NMAX / NT;
             float tv[PER], bv[PER];
 #pragma unroll
             for (int e = 0; e < PER; ++e) {
-                const int idx = tid + 128 * e;
+                const int idx = tid + NT * e;
                 const int r = idx % NMAX, c = idx / NMAX;
                 tv[e] = (r < ht && r < n && c < n) ? tile[r + c * p.ld] : 0.f;
                 if (p.P)
@@ -116,7 +129,7 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
             }
 #pragma unroll
             for (int e = 0; e < PER; ++e) {
-                const int idx = tid + 128 * e;
+                const int idx = tid + NT * e;
                 const int r = idx % NMAX, c = idx / NMAX;
                 S.Vt[r][c] = (r > c) ? tv[e] : ((r == c && c < n) ? 1.f : 0.f);
                 S.u.w.Tt[r][c] = (r <= c) ? tv[e] : 0.f;
@@ -128,8 +141,8 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
         // c0 .. c0+CPT-1: per term one shared load of its own operand and
         // CPT/4 16-byte loads of the other, which every lane of the warp
         // reads at the same address (broadcast).
-        constexpr int CPT = NMAX * NMAX / 128;
-        static_assert(CPT % 2 == 0 && CPT <= 8, "W products read 8- or 16-byte groups");
+        constexpr int CPT = NMAX * NMAX / NT;
+        static_assert(CPT % 2 == 0 && CPT <= 16, "W products read 8- or 16-byte groups");
         const int k = tid % NMAX, c0 = (tid / NMAX) * CPT;
         auto row_terms = [&](const float* row, float(&a)[CPT], float x) {
             if constexpr (CPT % 4 == 0) {
@@ -183,18 +196,18 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
         const int nblk = (ht + 127) / 128;
         __syncthreads();  // Vt complete (masked top rows)
         for (int blk = 0; blk < nblk; ++blk) {
-            const int r = blk * 128 + tid;
-            float v[NMAX];
+            const int r = blk * 128 + rb;
+            float v[HC];
 #pragma unroll
-            for (int k = 0; k < NMAX; ++k) v[k] = (r < n) ? S.Vt[r][k] : vnext[k];
+            for (int j = 0; j < HC; ++j) v[j] = (r < n) ? S.Vt[r][cb + j] : vnext[j];
 #pragma unroll
-            for (int k4 = 0; k4 < NMAX; k4 += 4) {
+            for (int k4 = 0; k4 < HC; k4 += 4) {
                 uint4 hi, lo;
                 tc::split_tf32(v[k4 + 0], hi.x, lo.x);
                 tc::split_tf32(v[k4 + 1], hi.y, lo.y);
                 tc::split_tf32(v[k4 + 2], hi.z, lo.z);
                 tc::split_tf32(v[k4 + 3], hi.w, lo.w);
-                const uint32_t off = tc::kmajor_off(tid, k4, NMAX);
+                const uint32_t off = tc::kmajor_off(rb, cb + k4, NMAX);
                 *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(S.u.op.a_hi) + off) = hi;
                 *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(S.u.op.a_lo) + off) = lo;
             }
@@ -230,12 +243,13 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
             }
             phase ^= 1u;
             tc::fence_after_sync();
-            // epilogue: warp w owns TMEM lanes 32w..32w+31 = rows of the block
-            float d[NMAX];
+            // epilogue: warp w owns TMEM lanes 32 (w % 4) .. +31 = rows rb
+            // of the block, columns cb .. cb + HC - 1
+            float d[HC];
 #pragma unroll
-            for (int c8 = 0; c8 < NMAX; c8 += 8) {
+            for (int c8 = 0; c8 < HC; c8 += 8) {
                 float d8[8];
-                tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c8, d8);
+                tc::tmem_ld8(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(cb + c8), d8);
 #pragma unroll
                 for (int e = 0; e < 8; ++e) d[c8 + e] = d8[e];
             }
@@ -243,12 +257,12 @@ __global__ void __launch_bounds__(128, NMAX <= 32 ? 4 : 1) tc_apply_tiles(ApplyP
             if (r < ht) {
                 if (r < n) {  // the top block: Q = B + D
 #pragma unroll
-                    for (int c = 0; c < NMAX; ++c)
-                        if (NF || c < n) tile[r + (int64_t)c * p.ld] = S.Bs[r][c] + d[c];
+                    for (int j = 0; j < HC; ++j)
+                        if (NF || cb + j < n) tile[r + (int64_t)(cb + j) * p.ld] = S.Bs[r][cb + j] + d[j];
                 } else {  // below it: Q = D
 #pragma unroll
-                    for (int c = 0; c < NMAX; ++c)
-                        if (NF || c < n) tile[r + (int64_t)c * p.ld] = d[c];
+                    for (int j = 0; j < HC; ++j)
+                        if (NF || cb + j < n) tile[r + (int64_t)(cb + j) * p.ld] = d[j];
                 }
             }
             tc::fence_before_sync();
@@ -274,10 +288,11 @@ void launch(const ApplyParams<float>& p, int grid, int* err, cudaStream_t s) {
         cudaFuncSetAttribute(tc_apply_tiles<NMAX, B, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
     const int tries = wait_tries().load(std::memory_order_relaxed);
+    constexpr int NT = tc_apply_threads<NMAX>();
     if (p.n == NMAX)
-        tc_apply_tiles<NMAX, B, true><<<grid, 128, smem, s>>>(p, err, tries);
+        tc_apply_tiles<NMAX, B, true><<<grid, NT, smem, s>>>(p, err, tries);
     else
-        tc_apply_tiles<NMAX, B, false><<<grid, 128, smem, s>>>(p, err, tries);
+        tc_apply_tiles<NMAX, B, false><<<grid, NT, smem, s>>>(p, err, tries);
 }
 
 }  // namespace
@@ -288,7 +303,9 @@ bool tc_apply_level(const ApplyParams<float>& p, int nmax, int rows, int* err, c
     const int sms = device_sm_count();
     const int64_t resident = (int64_t)sms * (nmax <= 32 ? 4 : 1);
     const int grid = (int)(p.ntiles < 1 ? 1 : (p.ntiles > resident ? resident : p.ntiles));
-    if (nmax == 32 && rows == 512) {
+    if (nmax == 64 && rows == 512) {
+        launch<64, 512>(p, grid, err, s);
+    } else if (nmax == 32 && rows == 512) {
         launch<32, 512>(p, grid, err, s);
     } else if (nmax == 16 && rows == 512) {
         launch<16, 512>(p, grid, err, s);

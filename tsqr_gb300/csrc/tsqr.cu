@@ -400,21 +400,9 @@ tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R
         ap.ntiles = lv[l].ntiles;
         ap.P = (l == L - 1) ? nullptr : lv[l + 1].M;
         ap.ldp = (l == L - 1) ? 0 : lv[l + 1].ld;
-        if (c.nmax <= 32) {
-            ap.vec = 0;
-            if (!tc_apply_level(ap, c.nmax, c.rows, err, s)) return TSQR_ERR_UNSUPPORTED;
-            log_launch(kTagTc + l, s);
-        } else {
-            // 32 < n <= 64: the CUDA-core apply runs instead.  The tensor-core
-            // apply at 64 columns needs 132 KB of shared memory and 247
-            // registers, so one CTA of 4 warps per SM, which cannot hide its
-            // O(n^3) W products and per-block chain: the whole call at
-            // 4,194,304 x 64 took 6.98 ms with it against 6.42 ms with this.
-            constexpr int ve = 4;
-            ap.vec = (lv[l].ld % ve == 0 && (reinterpret_cast<uintptr_t>(lv[l].M) % 16) == 0) ? 1 : 0;
-            c.ks.apply(ap, (int)std::min<int64_t>(lv[l].ntiles, 1 << 30), s);
-            log_launch(kTagApply + l, s);
-        }
+        ap.vec = 0;
+        if (!tc_apply_level(ap, c.nmax, c.rows, err, s)) return TSQR_ERR_UNSUPPORTED;
+        log_launch(kTagTc + l, s);
     }
     return cudaGetLastError() == cudaSuccess ? TSQR_OK : TSQR_ERR_CUDA;
 }
@@ -542,7 +530,7 @@ tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int
             const PrecLayout PL = prec_layout(m, n, c);
             ks = c.ks;
             nmax = c.nmax;
-            tc = c.nmax <= 32;
+            tc = true;
             err = reinterpret_cast<int*>(tw + PL.status);
             lvbase = tw + PL.levels;
         }
