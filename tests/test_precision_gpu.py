@@ -83,14 +83,21 @@ def test_precision_form_is_float_only(cuda, tg):
     assert torch.isfinite(R).all()
 
 
-@pytest.mark.parametrize("m,n,reorth", [(27648, 128, False), (20000, 96, False), (50000, 256, True)])
+@pytest.mark.parametrize("m,n,reorth", [(27648, 128, False), (20000, 96, False), (50000, 256, True),
+                                        (40000, 512, True), (30001, 520, False)])
 def test_blocked_qr_precision_form(orc, cuda, tg, m, n, reorth):
-    """qr with R12 = A1^T A2 and A2 -= A1 R12 on tcgen05 (TF32x3)."""
+    """qr with R12 = A1^T A2 and A2 -= A1 R12 in the precision form: the
+    256-wide node's projection on the TMA-fed tcgen05 kernel (n = 512, 520),
+    its update on tcgen05, the narrower products in FP32.  Bars: backward
+    error <= 1e-5; orthogonality <= 1e-5 up to 256 columns, and the FP32
+    bound 10 n u beyond (3.1e-4 at n = 512; block Gram-Schmidt's loss of
+    orthogonality grows with n in FP32 arithmetic too)."""
     A = orc.fill_uniform(m, n, np.float32, seed=12)
     dA = to_dev(tg, A)
     dR = tg.qr_(dA, precision="tf32x3", reorth=reorth)
     met = orc.metrics(A, to_host(dA), to_host(dR))
-    assert met["backward"] <= 1e-5 and met["orth"] <= 1e-5, met
+    orth_bar = 1e-5 if n <= 256 else 10 * n * 2.0 ** -24
+    assert met["backward"] <= 1e-5 and met["orth"] <= orth_bar, met
 
 
 def test_blocked_qr_precision_matches_plain(orc, cuda, tg):
@@ -171,12 +178,13 @@ def test_a_tensor_core_wait_that_runs_out_is_reported_and_the_next_call_succeeds
     in-flight MMAs retire (that wait keeps the full limit), frees its TMEM and
     returns, and the call's status word reads TSQR_ERR_CUDA.  Nothing is left
     broken: with the default limit restored the same calls succeed, clear the
-    word and meet the form's bar (<= 1e-5)."""
+    word and meet the form's bar (backward <= 1e-5; orthogonality <= 1e-5
+    for TSQR, 10 n u for the 512-column QR)."""
     import torch
     L = tg.lib()
     m, n = 70000, 32
     A = orc.fill_uniform(m, n, np.float32, seed=21)
-    m2, n2 = 20000, 256
+    m2, n2 = 20000, 512  # the 256-wide node: TMA-fed tcgen05 projection and tcgen05 update
     B = orc.fill_uniform(m2, n2, np.float32, seed=22)
     w = torch.zeros(tg.workspace_bytes(m, n, torch.float32, precision="tf32x3"), dtype=torch.uint8, device="cuda")
     w2 = torch.zeros(tg.qr_workspace_bytes(m2, n2, torch.float32, precision="tf32x3"), dtype=torch.uint8,
@@ -184,7 +192,7 @@ def test_a_tensor_core_wait_that_runs_out_is_reported_and_the_next_call_succeeds
     try:
         assert L.tsqr_debug_set_wait_limit(0) == 0
         tg.tsqr_(to_dev(tg, A), precision="tf32x3", work=w)        # tc_apply_tiles
-        tg.qr_(to_dev(tg, B), precision="tf32x3", work=w2)         # tc_gemm_kernel
+        tg.qr_(to_dev(tg, B), precision="tf32x3", work=w2)         # tc_tn_tma_kernel, tc_gemm_kernel
         torch.cuda.synchronize()
         assert L.tsqr_workspace_check(w.data_ptr()) == 4           # TSQR_ERR_CUDA
         assert L.tsqr_workspace_check(w2.data_ptr()) == 4
@@ -197,9 +205,11 @@ def test_a_tensor_core_wait_that_runs_out_is_reported_and_the_next_call_succeeds
     torch.cuda.synchronize()
     assert L.tsqr_workspace_check(w.data_ptr()) == 0
     assert L.tsqr_workspace_check(w2.data_ptr()) == 0
-    for M0, dQ, dRr in ((A, dA, dR), (B, dB, dR2)):
+    # the 512-column block Gram-Schmidt QR: orthogonality within the FP32
+    # bound 10 n u (3.1e-4)
+    for M0, dQ, dRr, orth_bar in ((A, dA, dR, 1e-5), (B, dB, dR2, 10 * n2 * 2.0 ** -24)):
         met = orc.metrics(M0, to_host(dQ), to_host(dRr))
-        assert met["backward"] <= 1e-5 and met["orth"] <= 1e-5, met
+        assert met["backward"] <= 1e-5 and met["orth"] <= orth_bar, met
 
 
 @pytest.mark.parametrize("m,n", [(27648, 32), (100000, 64), (70001, 13), (1000, 7), (300000, 16)])

@@ -35,6 +35,22 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
     return d;                // base offset 0, lbo mode 0, layout 0 = no swizzle
 }
 
+// The same for a K-major operand in the 128-byte swizzled layout that TMA
+// writes with CU_TENSOR_MAP_SWIZZLE_128B: rows of 128 bytes of K, 8-row
+// groups 1024 bytes apart (SBO), the leading offset unused (encoded 1),
+// layout type 2 (128-byte swizzle) in bits 61-63.  The buffer must be
+// 1024-byte aligned; a K step inside the 128-byte row advances the start
+// address, and the hardware applies the swizzle to the computed addresses.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;            // leading byte offset: unused for this layout
+    d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset: 8 rows x 128 bytes
+    d |= (uint64_t)1 << 46;            // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;            // 128-byte swizzle
+    return d;
+}
+
 // Instruction descriptor, kind::tf32: FP32 accumulator, TF32 A and B, both
 // K-major, M x N tile.
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {

@@ -322,11 +322,197 @@ void launch_nb(int nb, dim3 g, int M, int N, int64_t K, const float* A, int64_t 
 
 int nb_for(int N) { return N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256)); }
 
+// ---------------------------------------------------------------------------
+// P_z = A^T B (TF32x3) with the operands fed by TMA.  A (K x M) and B (K x N)
+// are column-major, so each is K-major as an MMA operand: a 32-row stage of
+// K arrives as boxes of 32 x 128 (A) and 32 x NB (B) with the 128-byte
+// swizzle, which is the layout the MMA reads (smem_desc_sw128).  The raw
+// FP32 tile is the hi operand (TF32 reads the top 19 bits); one pass of the
+// CTA writes lo = x - trunc(x) beside it at the same offsets, and one thread
+// issues hi*hi + hi*lo + lo*hi for the 4 K steps of 8.  Two stages: the
+// copy of stage s+2 is issued once the MMAs of stage s have read its
+// buffers.  Every wait is bounded; a CTA whose wait gives up sets the
+// status word, waits (with the full limit) for its copies and MMAs in
+// flight, frees its TMEM and stops.
+template <int NB>
+struct TnTma {
+    static constexpr int A_BYTES = 128 * 128;             // 128 rows of 32 FP32
+    static constexpr int B_BYTES = NB * 128;
+    static constexpr int RAW = A_BYTES + B_BYTES;          // raw A | raw B
+    static constexpr int STAGE = 2 * RAW;                  // then lo A | lo B
+    static constexpr size_t SMEM = 2 * (size_t)STAGE + 1024;
+};
+
+template <int NB>
+__global__ void __launch_bounds__(128, 1)
+    tc_tn_tma_kernel(int M, int N, int64_t K, int64_t kchunk, float* __restrict__ P,
+                     const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int* err,
+                     int tries) {
+    using L = TnTma<NB>;
+    extern __shared__ unsigned char tn_smem[];
+    __shared__ unsigned long long full[2], mmad[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int t0_failed;
+    unsigned char* base = tn_smem + ((1024 - (tc::smem_u32(tn_smem) & 1023)) & 1023);
+    const uint32_t sbase = tc::smem_u32(base);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.x * 128, n0 = blockIdx.y * NB;
+    const int64_t kbeg = (int64_t)blockIdx.z * kchunk;
+    const int64_t kend = K < kbeg + kchunk ? K : kbeg + kchunk;
+    const int nst = kend > kbeg ? (int)((kend - kbeg + 31) / 32) : 0;
+    constexpr uint32_t idesc = tc::idesc_tf32(128, NB);
+
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, NB);
+    if (tid == 0) {
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(tc::smem_u32(&full[b]), 1);
+            tc::mbar_init(tc::smem_u32(&mmad[b]), 1);
+        }
+        tc::fence_mbar_init();
+        t0_failed = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_slot;
+
+    // thread 0's record of what is in flight: copies issued (stages
+    // [0, issued)), MMA groups committed ([0, committed)) and waited ([0, mwaited))
+    int issued = 0, committed = 0, mwaited = 0;
+    auto issue = [&](int s) {
+        const int b = s & 1;
+        const uint32_t dst = sbase + b * L::STAGE, mb = tc::smem_u32(&full[b]);
+        const int x = (int)(kbeg + 32 * (int64_t)s);
+        tc::fence_smem_to_async();
+        tc::mbar_arrive_expect_tx(mb, L::RAW);
+        tc::tma_load_2d(dst, &ta, x, m0, mb);
+        tc::tma_load_2d(dst + L::A_BYTES, &tb, x, n0, mb);
+        issued = s + 1;
+    };
+    if (tid == 0) {
+        if (nst > 0) issue(0);
+        if (nst > 1) issue(1);
+    }
+    bool ok = true;
+    int s = 0;
+    for (; s < nst; ++s) {
+        const int b = s & 1;
+        const bool w = tc::mbar_wait(tc::smem_u32(&full[b]), (uint32_t)(s >> 1) & 1u, tries);
+        if (__syncthreads_or(!w || t0_failed)) {
+            ok = false;
+            break;
+        }
+        // lo = x - trunc_tf32(x), written beside the raw tile
+        {
+            const uint4* src = reinterpret_cast<const uint4*>(base + b * L::STAGE);
+            uint4* dst = reinterpret_cast<uint4*>(base + b * L::STAGE + L::RAW);
+#pragma unroll 4
+            for (int i = tid; i < L::RAW / 16; i += 128) {
+                const uint4 x = src[i];
+                uint4 lo;
+                lo.x = __float_as_uint(__uint_as_float(x.x) - __uint_as_float(x.x & 0xFFFFE000u));
+                lo.y = __float_as_uint(__uint_as_float(x.y) - __uint_as_float(x.y & 0xFFFFE000u));
+                lo.z = __float_as_uint(__uint_as_float(x.z) - __uint_as_float(x.z & 0xFFFFE000u));
+                lo.w = __float_as_uint(__uint_as_float(x.w) - __uint_as_float(x.w & 0xFFFFE000u));
+                dst[i] = lo;
+            }
+        }
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint32_t st = sbase + b * L::STAGE;
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+                const uint32_t ko = ks * 32;
+                const uint64_t ah = tc::smem_desc_sw128(st + ko), bh = tc::smem_desc_sw128(st + L::A_BYTES + ko);
+                const uint64_t al = tc::smem_desc_sw128(st + L::RAW + ko),
+                               bl = tc::smem_desc_sw128(st + L::RAW + L::A_BYTES + ko);
+                tc::mma_tf32(tmem, ah, bh, idesc, (s > 0) || (ks > 0));
+                tc::mma_tf32(tmem, ah, bl, idesc, true);
+                tc::mma_tf32(tmem, al, bh, idesc, true);
+            }
+            tc::mma_commit(tc::smem_u32(&mmad[b]));
+            committed = s + 1;
+            if (s + 2 < nst) {
+                // the copy of stage s+2 overwrites buffer b: the MMAs of
+                // stage s read it
+                if (tc::mbar_wait(tc::smem_u32(&mmad[b]), (uint32_t)(s >> 1) & 1u, tries)) {
+                    mwaited = s + 1;
+                    issue(s + 2);
+                } else {
+                    t0_failed = 1;
+                }
+            }
+        }
+    }
+    if (ok && nst > 0) {
+        // the last one or two MMA groups (never waited for in the loop)
+        bool w0 = true;
+        const int first = nst >= 2 ? nst - 2 : 0;
+        for (int q = first; q < nst; ++q)
+            w0 = tc::mbar_wait(tc::smem_u32(&mmad[q & 1]), (uint32_t)(q >> 1) & 1u, tries) && w0;
+        if (__syncthreads_or(!w0)) ok = false;
+        else if (tid == 0) mwaited = nst;
+    }
+    if (!ok) {
+        if (tid == 0) {
+            if (err) atomicExch(err, 1);
+            // every copy and MMA group still in flight, with the full limit
+            for (int q = s; q < issued; ++q)
+                (void)tc::mbar_wait(tc::smem_u32(&full[q & 1]), (uint32_t)(q >> 1) & 1u);
+            for (int q = mwaited; q < committed; ++q)
+                (void)tc::mbar_wait(tc::smem_u32(&mmad[q & 1]), (uint32_t)(q >> 1) & 1u);
+        }
+    } else {
+        tc::fence_after_sync();
+        const int m = m0 + 32 * warp + (tid & 31);
+        float* Pz = P + (int64_t)blockIdx.z * M * N;
+#pragma unroll 2
+        for (int c8 = 0; c8 < NB; c8 += 8) {
+            float d[8];
+            tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c8, d);
+            tc::tmem_ld_wait();
+            if (m < M) {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int nn = n0 + c8 + e;
+                    if (nn < N) Pz[m + (int64_t)nn * M] = nst > 0 ? d[e] : 0.f;
+                }
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, NB);
+}
+
+template <int NB>
+bool launch_tn_tma(dim3 g, int M, int N, int64_t K, int64_t kchunk, const float* A, int64_t lda, const float* B,
+                   int64_t ldb, float* P, int* err, cudaStream_t s) {
+    CUtensorMap ta, tb;
+    if (K + 64 > INT32_MAX || !tensor_map_f32(&ta, A, lda, K, M, 32, 128, true) ||
+        !tensor_map_f32(&tb, B, ldb, K, N, 32, NB, true))
+        return false;
+    static PerDeviceOnce attr;
+    attr.run([] {
+        cudaFuncSetAttribute(tc_tn_tma_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TnTma<NB>::SMEM);
+    });
+    tc_tn_tma_kernel<NB><<<g, 128, TnTma<NB>::SMEM, s>>>(M, N, K, kchunk, P, ta, tb, err,
+                                                         wait_tries().load(std::memory_order_relaxed));
+    return true;
+}
+
 }  // namespace
 
 int tc_tn_splits(int64_t M, int64_t N, int64_t K) {
+    // one wave of one CTA per SM on GB300's 152 SMs (the TMA form's 192 KB
+    // of shared memory); the workspace query uses the same count
     const int64_t tiles = ((M + 127) / 128) * ((N + 255) / 256);
-    int64_t nz = std::max<int64_t>(1, (2 * 152 + tiles - 1) / tiles);
+    int64_t nz = std::max<int64_t>(1, (152 + tiles - 1) / tiles);
     nz = std::min<int64_t>(nz, std::max<int64_t>(1, K / 1024));
     return (int)nz;
 }
@@ -342,10 +528,18 @@ int tc_gemm_tn(int M, int N, int64_t K, const float* A, int64_t lda, const float
     const int nzr = (int)((K + kchunk - 1) / kchunk);
     const int nb = nb_for(std::min(N, 256));
     dim3 g((unsigned)((M + 127) / 128), (unsigned)((N + nb - 1) / nb), (unsigned)nzr);
-    if (bf16)
+    if (bf16) {
         launch_nb<true, true>(nb, g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s);
-    else
-        launch_nb<true, false>(nb, g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s);
+        return nzr;
+    }
+    bool done = false;
+    switch (nb) {
+        case 32: done = launch_tn_tma<32>(g, M, N, K, kchunk, A, lda, B, ldb, P, err, s); break;
+        case 64: done = launch_tn_tma<64>(g, M, N, K, kchunk, A, lda, B, ldb, P, err, s); break;
+        case 128: done = launch_tn_tma<128>(g, M, N, K, kchunk, A, lda, B, ldb, P, err, s); break;
+        default: done = launch_tn_tma<256>(g, M, N, K, kchunk, A, lda, B, ldb, P, err, s); break;
+    }
+    if (!done) launch_nb<true, false>(nb, g, M, N, K, A, lda, B, ldb, P, M, 1.f, kchunk, err, s);
     return nzr;
 }
 
