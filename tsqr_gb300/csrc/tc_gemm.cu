@@ -489,6 +489,226 @@ __global__ void __launch_bounds__(128, 1)
     if (warp == 0) tc::tmem_dealloc(tmem, NB);
 }
 
+// ---------------------------------------------------------------------------
+// C (M x N) += alpha A (M x K) B (K x N), TF32x3, A tall (the blocked QR's
+// update A2 -= A1 X).  B is K-major in memory (X column-major) and arrives by
+// TMA in the MMA's 128-byte swizzled K-major layout, raw FP32 as hi, lo
+// written beside it.  A is MN-major in memory (rows contiguous): each
+// 128 x 32 stage arrives as four 32 x 32 boxes with the 128-byte swizzle
+// (element (r, k) at (r/32) 4096 + k 128 + 16 ((r%32)/4 ^ k%8) + 4 (r%4)),
+// and the CTA rewrites it as K-major hi and lo tiles (element (r, k) at
+// r 128 + 16 (k/4 ^ r%8) + 4 (k%4)): lane l takes K index l and 4 rows per
+// 16-byte read, so the reads take the four wavefronts a 512-byte warp read
+// needs anyway and each 4-byte store of the warp hits 32 distinct banks.
+// hi = trunc(x) (the TF32 bits), lo = x - hi.  A persistent CTA (one per
+// SM) walks 128-row blocks; a block's K stages accumulate in TMEM, and its
+// epilogue reads C, adds alpha D and writes it back.  Two stages of copies
+// on mbarriers, bounded waits as in the projection kernel.
+template <int NB>
+struct NnTma {
+    static constexpr int A_RAW = 128 * 128;            // four 32 x 32 boxes
+    static constexpr int B_RAW = NB * 128;
+    static constexpr int RAW = A_RAW + B_RAW;
+    static constexpr int A_OP = 128 * 128;             // K-major hi (and lo)
+    static constexpr int STAGE = RAW + 2 * A_OP + B_RAW;  // raw A | raw B | A hi | A lo | B lo
+    static constexpr size_t SMEM = 2 * (size_t)STAGE + 1024;
+};
+
+template <int NB>
+__global__ void __launch_bounds__(128, 1)
+    tc_nn_tma_kernel(int64_t M, int N, int K, float alpha, float* __restrict__ C, int64_t ldc,
+                     const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int* err,
+                     int tries) {
+    using L = NnTma<NB>;
+    extern __shared__ unsigned char nn_smem[];
+    __shared__ unsigned long long full[2], mmad[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int t0_failed;
+    unsigned char* base = nn_smem + ((1024 - (tc::smem_u32(nn_smem) & 1023)) & 1023);
+    const uint32_t sbase = tc::smem_u32(base);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n0 = blockIdx.x * NB;
+    const int64_t nblk = (M + 127) / 128;
+    const int nks = (K + 31) / 32;
+    // this CTA's blocks: blockIdx.y, + gridDim.y, ...; steps t = (block j, stage s)
+    const int64_t myblk = nblk > blockIdx.y ? (nblk - 1 - blockIdx.y) / gridDim.y + 1 : 0;
+    const int64_t T = myblk * nks;
+    constexpr uint32_t idesc = tc::idesc_tf32(128, NB);
+
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, NB);
+    if (tid == 0) {
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(tc::smem_u32(&full[b]), 1);
+            tc::mbar_init(tc::smem_u32(&mmad[b]), 1);
+        }
+        tc::fence_mbar_init();
+        t0_failed = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_slot;
+
+    int64_t issued = 0, committed = 0, mwaited = 0;  // thread 0's record, as in the projection kernel
+    auto issue = [&](int64_t t) {
+        const int b = (int)(t & 1);
+        const int64_t j = t / nks;
+        const int s = (int)(t % nks);
+        const int r0 = (int)((blockIdx.y + j * gridDim.y) * 128);
+        const uint32_t dst = sbase + b * L::STAGE, mb = tc::smem_u32(&full[b]);
+        tc::fence_smem_to_async();
+        tc::mbar_arrive_expect_tx(mb, L::RAW);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tc::tma_load_2d(dst + q * 4096, &ta, r0 + 32 * q, 32 * s, mb);
+        tc::tma_load_2d(dst + L::A_RAW, &tb, 32 * s, n0, mb);
+        issued = t + 1;
+    };
+    if (tid == 0) {
+        if (T > 0) issue(0);
+        if (T > 1) issue(1);
+    }
+    bool ok = true;
+    int64_t t = 0;
+    for (; t < T; ++t) {
+        const int b = (int)(t & 1);
+        const int s = (int)(t % nks);
+        const bool w = tc::mbar_wait(tc::smem_u32(&full[b]), (uint32_t)(t >> 1) & 1u, tries);
+        if (__syncthreads_or(!w || t0_failed)) {
+            ok = false;
+            break;
+        }
+        unsigned char* st = base + b * L::STAGE;
+        {
+            // A: MN-major raw -> K-major hi, lo; lane = K index, 8 groups of 4 rows per warp
+            const unsigned char* ra = st;
+            unsigned char* ah = st + L::RAW;
+            unsigned char* al = ah + L::A_OP;
+            const int k = lane;
+#pragma unroll 4
+            for (int i = 0; i < 8; ++i) {
+                const int g = warp * 8 + i, r = 4 * g;  // rows r .. r + 3
+                const uint4 x = *reinterpret_cast<const uint4*>(ra + (r >> 5) * 4096 + k * 128 +
+                                                                ((((r & 31) >> 2) ^ (k & 7)) << 4));
+                const uint32_t xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int rr = r + q;
+                    const uint32_t off = rr * 128 + ((((k >> 2) ^ (rr & 7))) << 4) + (k & 3) * 4;
+                    const uint32_t hi = xv[q] & 0xFFFFE000u;
+                    *reinterpret_cast<uint32_t*>(ah + off) = hi;
+                    *reinterpret_cast<float*>(al + off) = __uint_as_float(xv[q]) - __uint_as_float(hi);
+                }
+            }
+            // B: lo beside the raw (hi) tile, same offsets
+            const uint4* rb = reinterpret_cast<const uint4*>(st + L::A_RAW);
+            uint4* bl = reinterpret_cast<uint4*>(st + L::RAW + 2 * L::A_OP);
+#pragma unroll 4
+            for (int i = tid; i < L::B_RAW / 16; i += 128) {
+                const uint4 x = rb[i];
+                uint4 lo;
+                lo.x = __float_as_uint(__uint_as_float(x.x) - __uint_as_float(x.x & 0xFFFFE000u));
+                lo.y = __float_as_uint(__uint_as_float(x.y) - __uint_as_float(x.y & 0xFFFFE000u));
+                lo.z = __float_as_uint(__uint_as_float(x.z) - __uint_as_float(x.z & 0xFFFFE000u));
+                lo.w = __float_as_uint(__uint_as_float(x.w) - __uint_as_float(x.w & 0xFFFFE000u));
+                bl[i] = lo;
+            }
+        }
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint32_t sa = sbase + b * L::STAGE;
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+                const uint32_t ko = ks * 32;
+                const uint64_t ah = tc::smem_desc_sw128(sa + L::RAW + ko);
+                const uint64_t al = tc::smem_desc_sw128(sa + L::RAW + L::A_OP + ko);
+                const uint64_t bh = tc::smem_desc_sw128(sa + L::A_RAW + ko);
+                const uint64_t bl = tc::smem_desc_sw128(sa + L::RAW + 2 * L::A_OP + ko);
+                tc::mma_tf32(tmem, ah, bh, idesc, (s > 0) || (ks > 0));
+                tc::mma_tf32(tmem, ah, bl, idesc, true);
+                tc::mma_tf32(tmem, al, bh, idesc, true);
+            }
+            tc::mma_commit(tc::smem_u32(&mmad[b]));
+            committed = t + 1;
+            if (t + 2 < T) {
+                if (tc::mbar_wait(tc::smem_u32(&mmad[b]), (uint32_t)(t >> 1) & 1u, tries)) {
+                    mwaited = t + 1;
+                    issue(t + 2);
+                } else {
+                    t0_failed = 1;
+                }
+            }
+        }
+        if (s == nks - 1) {
+            // the block's last stage: its MMAs done, C += alpha D
+            const bool wd = tc::mbar_wait(tc::smem_u32(&mmad[b]), (uint32_t)(t >> 1) & 1u, tries);
+            if (__syncthreads_or(!wd)) {
+                ok = false;
+                ++t;  // stage t was consumed
+                break;
+            }
+            if (tid == 0 && mwaited < t + 1) mwaited = t + 1;
+            tc::fence_after_sync();
+            const int64_t j = t / nks;
+            const int64_t m = (blockIdx.y + j * gridDim.y) * 128 + 32 * warp + lane;
+#pragma unroll 2
+            for (int c8 = 0; c8 < NB; c8 += 8) {
+                float d[8];
+                tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c8, d);
+                tc::tmem_ld_wait();
+                if (m < M) {
+                    float c[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const int nn = n0 + c8 + e;
+                        c[e] = (nn < N) ? C[m + (int64_t)nn * ldc] : 0.f;
+                    }
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const int nn = n0 + c8 + e;
+                        if (nn < N) C[m + (int64_t)nn * ldc] = c[e] + alpha * d[e];
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            __syncthreads();  // TMEM is read: the next block's MMAs may overwrite it
+        }
+    }
+    if (!ok && tid == 0) {
+        if (err) atomicExch(err, 1);
+        for (int64_t q = t; q < issued; ++q)
+            (void)tc::mbar_wait(tc::smem_u32(&full[q & 1]), (uint32_t)(q >> 1) & 1u);
+        for (int64_t q = mwaited; q < committed; ++q)
+            (void)tc::mbar_wait(tc::smem_u32(&mmad[q & 1]), (uint32_t)(q >> 1) & 1u);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, NB);
+}
+
+template <int NB>
+bool launch_nn_tma(int64_t M, int N, int K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb,
+                   float* C, int64_t ldc, int* err, cudaStream_t s) {
+    CUtensorMap ta, tb;
+    if (M + 128 > INT32_MAX || !tensor_map_f32(&ta, A, lda, M, K, 32, 32, true) ||
+        !tensor_map_f32(&tb, B, ldb, K, N, 32, NB, true))
+        return false;
+    static PerDeviceOnce attr;
+    attr.run([] {
+        cudaFuncSetAttribute(tc_nn_tma_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)NnTma<NB>::SMEM);
+    });
+    const int ntn = (N + NB - 1) / NB;
+    const int64_t nblk = (M + 127) / 128;
+    const int gy = (int)std::max<int64_t>(1, std::min<int64_t>(nblk, (device_sm_count() + ntn - 1) / ntn));
+    tc_nn_tma_kernel<NB><<<dim3((unsigned)ntn, (unsigned)gy), 128, NnTma<NB>::SMEM, s>>>(
+        M, N, K, alpha, C, ldc, ta, tb, err, wait_tries().load(std::memory_order_relaxed));
+    return true;
+}
+
 template <int NB>
 bool launch_tn_tma(dim3 g, int M, int N, int64_t K, int64_t kchunk, const float* A, int64_t lda, const float* B,
                    int64_t ldb, float* P, int* err, cudaStream_t s) {
@@ -549,10 +769,18 @@ void tc_gemm_nn(int64_t M, int N, int K, float alpha, const float* A, int64_t ld
                 float* C, int64_t ldc, int* err, cudaStream_t s, bool bf16) {
     const int nb = nb_for(std::min(N, 256));
     dim3 g((unsigned)((M + 127) / 128), (unsigned)((N + nb - 1) / nb), 1);
-    if (bf16)
+    if (bf16) {
         launch_nb<false, true>(nb, g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s);
-    else
-        launch_nb<false, false>(nb, g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s);
+        return;
+    }
+    // the TMA-fed form in N tiles of at most 128 (two stages of 160 KB)
+    bool done = false;
+    switch (nb) {
+        case 32: done = launch_nn_tma<32>(M, N, K, alpha, A, lda, B, ldb, C, ldc, err, s); break;
+        case 64: done = launch_nn_tma<64>(M, N, K, alpha, A, lda, B, ldb, C, ldc, err, s); break;
+        default: done = launch_nn_tma<128>(M, N, K, alpha, A, lda, B, ldb, C, ldc, err, s); break;
+    }
+    if (!done) launch_nb<false, false>(nb, g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s);
 }
 
 }  // namespace tsqr
