@@ -500,18 +500,24 @@ __global__ void __launch_bounds__(128, 1)
 // r 128 + 16 (k/4 ^ r%8) + 4 (k%4)): lane l takes K index l and 4 rows per
 // 16-byte read, so the reads take the four wavefronts a 512-byte warp read
 // needs anyway and each 4-byte store of the warp hits 32 distinct banks.
-// hi = trunc(x) (the TF32 bits), lo = x - hi.  A persistent CTA (one per
-// SM) walks 128-row blocks; a block's K stages accumulate in TMEM, and its
-// epilogue reads C, adds alpha D and writes it back.  Two stages of copies
-// on mbarriers, bounded waits as in the projection kernel.
+// hi = trunc(x) (the TF32 bits), lo = x - hi, for B as well, so that a
+// copy's buffer is free once the CTA has rewritten it: the copies run in a
+// ring of three stages (the copy of step t+3 is issued right after step t's
+// rewrite), the operand tiles in two buffers (step t's rewrite waits for the
+// MMAs of step t-2).  A persistent CTA (one per SM) walks 128-row blocks; a
+// block's K stages accumulate in TMEM, and its epilogue reads C 32 columns
+// at a time, adds alpha D and writes it back.  Bounded waits as in the
+// projection kernel.
 template <int NB>
 struct NnTma {
     static constexpr int A_RAW = 128 * 128;            // four 32 x 32 boxes
     static constexpr int B_RAW = NB * 128;
-    static constexpr int RAW = A_RAW + B_RAW;
-    static constexpr int A_OP = 128 * 128;             // K-major hi (and lo)
-    static constexpr int STAGE = RAW + 2 * A_OP + B_RAW;  // raw A | raw B | A hi | A lo | B lo
-    static constexpr size_t SMEM = 2 * (size_t)STAGE + 1024;
+    static constexpr int RAW = A_RAW + B_RAW;          // one raw stage (TMA destination)
+    static constexpr int A_OP = 128 * 128;             // one K-major operand tile of A
+    static constexpr int B_OP = NB * 128;
+    static constexpr int OPS = 2 * A_OP + 2 * B_OP;    // A hi | A lo | B hi | B lo
+    static constexpr int NRAW = 3;                     // raw ring depth
+    static constexpr size_t SMEM = NRAW * (size_t)RAW + 2 * (size_t)OPS + 1024;
 };
 
 template <int NB>
@@ -521,11 +527,11 @@ __global__ void __launch_bounds__(128, 1)
                      int tries) {
     using L = NnTma<NB>;
     extern __shared__ unsigned char nn_smem[];
-    __shared__ unsigned long long full[2], mmad[2];
+    __shared__ unsigned long long full[L::NRAW], mmad[2];
     __shared__ uint32_t tmem_slot;
-    __shared__ int t0_failed;
     unsigned char* base = nn_smem + ((1024 - (tc::smem_u32(nn_smem) & 1023)) & 1023);
     const uint32_t sbase = tc::smem_u32(base);
+    unsigned char* opsbase = base + L::NRAW * L::RAW;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n0 = blockIdx.x * NB;
     const int64_t nblk = (M + 127) / 128;
@@ -537,25 +543,22 @@ __global__ void __launch_bounds__(128, 1)
 
     if (warp == 0) tc::tmem_alloc(&tmem_slot, NB);
     if (tid == 0) {
-        for (int b = 0; b < 2; ++b) {
-            tc::mbar_init(tc::smem_u32(&full[b]), 1);
-            tc::mbar_init(tc::smem_u32(&mmad[b]), 1);
-        }
+        for (int b = 0; b < L::NRAW; ++b) tc::mbar_init(tc::smem_u32(&full[b]), 1);
+        for (int b = 0; b < 2; ++b) tc::mbar_init(tc::smem_u32(&mmad[b]), 1);
         tc::fence_mbar_init();
-        t0_failed = 0;
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_slot;
 
-    int64_t issued = 0, committed = 0, mwaited = 0;  // thread 0's record, as in the projection kernel
+    int64_t issued = 0, committed = 0;  // thread 0: copies issued for steps [0, issued), MMA groups committed
     auto issue = [&](int64_t t) {
-        const int b = (int)(t & 1);
+        const int rb = (int)(t % L::NRAW);
         const int64_t j = t / nks;
         const int s = (int)(t % nks);
         const int r0 = (int)((blockIdx.y + j * gridDim.y) * 128);
-        const uint32_t dst = sbase + b * L::STAGE, mb = tc::smem_u32(&full[b]);
+        const uint32_t dst = sbase + rb * L::RAW, mb = tc::smem_u32(&full[rb]);
         tc::fence_smem_to_async();
         tc::mbar_arrive_expect_tx(mb, L::RAW);
 #pragma unroll
@@ -563,26 +566,28 @@ __global__ void __launch_bounds__(128, 1)
         tc::tma_load_2d(dst + L::A_RAW, &tb, 32 * s, n0, mb);
         issued = t + 1;
     };
-    if (tid == 0) {
-        if (T > 0) issue(0);
-        if (T > 1) issue(1);
-    }
+    if (tid == 0)
+        for (int64_t q = 0; q < L::NRAW && q < T; ++q) issue(q);
     bool ok = true;
     int64_t t = 0;
     for (; t < T; ++t) {
-        const int b = (int)(t & 1);
+        const int rb = (int)(t % L::NRAW), ob = (int)(t & 1);
         const int s = (int)(t % nks);
-        const bool w = tc::mbar_wait(tc::smem_u32(&full[b]), (uint32_t)(t >> 1) & 1u, tries);
-        if (__syncthreads_or(!w || t0_failed)) {
+        // the stage's copy has landed, and the MMAs of step t-2 (which read
+        // operand buffer ob) are done
+        bool w = tc::mbar_wait(tc::smem_u32(&full[rb]), (uint32_t)((t / L::NRAW) & 1), tries);
+        if (t >= 2) w = tc::mbar_wait(tc::smem_u32(&mmad[ob]), (uint32_t)((t - 2) >> 1) & 1u, tries) && w;
+        if (__syncthreads_or(!w)) {
             ok = false;
             break;
         }
-        unsigned char* st = base + b * L::STAGE;
+        const unsigned char* ra = base + rb * L::RAW;
+        unsigned char* ah = opsbase + ob * L::OPS;
+        unsigned char* al = ah + L::A_OP;
+        unsigned char* bh = al + L::A_OP;
+        unsigned char* bl = bh + L::B_OP;
         {
             // A: MN-major raw -> K-major hi, lo; lane = K index, 8 groups of 4 rows per warp
-            const unsigned char* ra = st;
-            unsigned char* ah = st + L::RAW;
-            unsigned char* al = ah + L::A_OP;
             const int k = lane;
 #pragma unroll 4
             for (int i = 0; i < 8; ++i) {
@@ -599,76 +604,80 @@ __global__ void __launch_bounds__(128, 1)
                     *reinterpret_cast<float*>(al + off) = __uint_as_float(xv[q]) - __uint_as_float(hi);
                 }
             }
-            // B: lo beside the raw (hi) tile, same offsets
-            const uint4* rb = reinterpret_cast<const uint4*>(st + L::A_RAW);
-            uint4* bl = reinterpret_cast<uint4*>(st + L::RAW + 2 * L::A_OP);
+            // B: already K-major; hi and lo at the same offsets
+            const uint4* rbp = reinterpret_cast<const uint4*>(ra + L::A_RAW);
+            uint4* bhp = reinterpret_cast<uint4*>(bh);
+            uint4* blp = reinterpret_cast<uint4*>(bl);
 #pragma unroll 4
             for (int i = tid; i < L::B_RAW / 16; i += 128) {
-                const uint4 x = rb[i];
-                uint4 lo;
-                lo.x = __float_as_uint(__uint_as_float(x.x) - __uint_as_float(x.x & 0xFFFFE000u));
-                lo.y = __float_as_uint(__uint_as_float(x.y) - __uint_as_float(x.y & 0xFFFFE000u));
-                lo.z = __float_as_uint(__uint_as_float(x.z) - __uint_as_float(x.z & 0xFFFFE000u));
-                lo.w = __float_as_uint(__uint_as_float(x.w) - __uint_as_float(x.w & 0xFFFFE000u));
-                bl[i] = lo;
+                const uint4 x = rbp[i];
+                uint4 h, lo;
+                h.x = x.x & 0xFFFFE000u;
+                h.y = x.y & 0xFFFFE000u;
+                h.z = x.z & 0xFFFFE000u;
+                h.w = x.w & 0xFFFFE000u;
+                lo.x = __float_as_uint(__uint_as_float(x.x) - __uint_as_float(h.x));
+                lo.y = __float_as_uint(__uint_as_float(x.y) - __uint_as_float(h.y));
+                lo.z = __float_as_uint(__uint_as_float(x.z) - __uint_as_float(h.z));
+                lo.w = __float_as_uint(__uint_as_float(x.w) - __uint_as_float(h.w));
+                bhp[i] = h;
+                blp[i] = lo;
             }
         }
         tc::fence_smem_to_async();
         tc::fence_before_sync();
-        __syncthreads();
+        __syncthreads();  // raw buffer rb consumed, operand buffer ob written
         if (tid == 0) {
             tc::fence_after_sync();
-            const uint32_t sa = sbase + b * L::STAGE;
+            if (t + L::NRAW < T) issue(t + L::NRAW);
+            const uint32_t so = tc::smem_u32(ah);
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks) {
                 const uint32_t ko = ks * 32;
-                const uint64_t ah = tc::smem_desc_sw128(sa + L::RAW + ko);
-                const uint64_t al = tc::smem_desc_sw128(sa + L::RAW + L::A_OP + ko);
-                const uint64_t bh = tc::smem_desc_sw128(sa + L::A_RAW + ko);
-                const uint64_t bl = tc::smem_desc_sw128(sa + L::RAW + 2 * L::A_OP + ko);
-                tc::mma_tf32(tmem, ah, bh, idesc, (s > 0) || (ks > 0));
-                tc::mma_tf32(tmem, ah, bl, idesc, true);
-                tc::mma_tf32(tmem, al, bh, idesc, true);
+                const uint64_t dah = tc::smem_desc_sw128(so + ko);
+                const uint64_t dal = tc::smem_desc_sw128(so + L::A_OP + ko);
+                const uint64_t dbh = tc::smem_desc_sw128(so + 2 * L::A_OP + ko);
+                const uint64_t dbl = tc::smem_desc_sw128(so + 2 * L::A_OP + L::B_OP + ko);
+                tc::mma_tf32(tmem, dah, dbh, idesc, (s > 0) || (ks > 0));
+                tc::mma_tf32(tmem, dah, dbl, idesc, true);
+                tc::mma_tf32(tmem, dal, dbh, idesc, true);
             }
-            tc::mma_commit(tc::smem_u32(&mmad[b]));
+            tc::mma_commit(tc::smem_u32(&mmad[ob]));
             committed = t + 1;
-            if (t + 2 < T) {
-                if (tc::mbar_wait(tc::smem_u32(&mmad[b]), (uint32_t)(t >> 1) & 1u, tries)) {
-                    mwaited = t + 1;
-                    issue(t + 2);
-                } else {
-                    t0_failed = 1;
-                }
-            }
         }
         if (s == nks - 1) {
             // the block's last stage: its MMAs done, C += alpha D
-            const bool wd = tc::mbar_wait(tc::smem_u32(&mmad[b]), (uint32_t)(t >> 1) & 1u, tries);
+            const bool wd = tc::mbar_wait(tc::smem_u32(&mmad[ob]), (uint32_t)(t >> 1) & 1u, tries);
             if (__syncthreads_or(!wd)) {
                 ok = false;
                 ++t;  // stage t was consumed
                 break;
             }
-            if (tid == 0 && mwaited < t + 1) mwaited = t + 1;
             tc::fence_after_sync();
             const int64_t j = t / nks;
             const int64_t m = (blockIdx.y + j * gridDim.y) * 128 + 32 * warp + lane;
-#pragma unroll 2
-            for (int c8 = 0; c8 < NB; c8 += 8) {
-                float d[8];
-                tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c8, d);
+#pragma unroll 1
+            for (int c32 = 0; c32 < NB; c32 += 32) {
+                // 32 columns per round: the TMEM reads and the 32 loads of C
+                // are all in flight before the first store
+                float d[32], c[32];
+#pragma unroll
+                for (int c8 = 0; c8 < 32 && c32 + c8 < NB; c8 += 8)
+                    tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(c32 + c8),
+                                 *reinterpret_cast<float(*)[8]>(d + c8));
+                if (m < M) {
+#pragma unroll
+                    for (int e = 0; e < 32; ++e) {
+                        const int nn = n0 + c32 + e;
+                        c[e] = (c32 + e < NB && nn < N) ? C[m + (int64_t)nn * ldc] : 0.f;
+                    }
+                }
                 tc::tmem_ld_wait();
                 if (m < M) {
-                    float c[8];
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        const int nn = n0 + c8 + e;
-                        c[e] = (nn < N) ? C[m + (int64_t)nn * ldc] : 0.f;
-                    }
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        const int nn = n0 + c8 + e;
-                        if (nn < N) C[m + (int64_t)nn * ldc] = c[e] + alpha * d[e];
+                    for (int e = 0; e < 32; ++e) {
+                        const int nn = n0 + c32 + e;
+                        if (c32 + e < NB && nn < N) C[m + (int64_t)nn * ldc] = c[e] + alpha * d[e];
                     }
                 }
             }
@@ -676,12 +685,15 @@ __global__ void __launch_bounds__(128, 1)
             __syncthreads();  // TMEM is read: the next block's MMAs may overwrite it
         }
     }
-    if (!ok && tid == 0) {
-        if (err) atomicExch(err, 1);
-        for (int64_t q = t; q < issued; ++q)
-            (void)tc::mbar_wait(tc::smem_u32(&full[q & 1]), (uint32_t)(q >> 1) & 1u);
-        for (int64_t q = mwaited; q < committed; ++q)
-            (void)tc::mbar_wait(tc::smem_u32(&mmad[q & 1]), (uint32_t)(q >> 1) & 1u);
+    if (!ok) {
+        if (tid == 0) {
+            if (err) atomicExch(err, 1);
+            // every copy and MMA group still in flight, with the full limit
+            for (int64_t q = t; q < issued; ++q)
+                (void)tc::mbar_wait(tc::smem_u32(&full[q % L::NRAW]), (uint32_t)((q / L::NRAW) & 1));
+            for (int64_t q = committed >= 2 ? committed - 2 : 0; q < committed; ++q)
+                (void)tc::mbar_wait(tc::smem_u32(&mmad[q & 1]), (uint32_t)(q >> 1) & 1u);
+        }
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -773,7 +785,7 @@ void tc_gemm_nn(int64_t M, int N, int K, float alpha, const float* A, int64_t ld
         launch_nb<false, true>(nb, g, (int)M, N, K, A, lda, B, ldb, C, ldc, alpha, 0, err, s);
         return;
     }
-    // the TMA-fed form in N tiles of at most 128 (two stages of 160 KB)
+    // the TMA-fed form in N tiles of at most 128 (225 KB of shared memory)
     bool done = false;
     switch (nb) {
         case 32: done = launch_nn_tma<32>(M, N, K, alpha, A, lda, B, ldb, C, ldc, err, s); break;
