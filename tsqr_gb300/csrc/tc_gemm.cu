@@ -500,7 +500,7 @@ __global__ void __launch_bounds__(128, 1)
 // r 128 + 16 (k/4 ^ r%8) + 4 (k%4)): lane l takes K index l and 4 rows per
 // 16-byte read, so the reads take the four wavefronts a 512-byte warp read
 // needs anyway and each 4-byte store of the warp hits 32 distinct banks.
-// hi = trunc(x) (the TF32 bits), lo = x - hi, for B as well, so that a
+// hi = x rounded to TF32, lo = the rest, for B as well, so that a
 // copy's buffer is free once the CTA has rewritten it: the copies run in a
 // ring of three stages (the copy of step t+3 is issued right after step t's
 // rewrite), the operand tiles in two buffers (step t's rewrite waits for the
@@ -521,7 +521,7 @@ struct NnTma {
 };
 
 template <int NB>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(256, 1)
     tc_nn_tma_kernel(int64_t M, int N, int K, float alpha, float* __restrict__ C, int64_t ldc,
                      const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int* err,
                      int tries) {
@@ -587,11 +587,11 @@ __global__ void __launch_bounds__(128, 1)
         unsigned char* bh = al + L::A_OP;
         unsigned char* bl = bh + L::B_OP;
         {
-            // A: MN-major raw -> K-major hi, lo; lane = K index, 8 groups of 4 rows per warp
+            // A: MN-major raw -> K-major hi, lo; lane = K index, 4 groups of 4 rows per warp
             const int k = lane;
-#pragma unroll 4
-            for (int i = 0; i < 8; ++i) {
-                const int g = warp * 8 + i, r = 4 * g;  // rows r .. r + 3
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int g = warp * 4 + i, r = 4 * g;  // rows r .. r + 3
                 const uint4 x = *reinterpret_cast<const uint4*>(ra + (r >> 5) * 4096 + k * 128 +
                                                                 ((((r & 31) >> 2) ^ (k & 7)) << 4));
                 const uint32_t xv[4] = {x.x, x.y, x.z, x.w};
@@ -599,9 +599,10 @@ __global__ void __launch_bounds__(128, 1)
                 for (int q = 0; q < 4; ++q) {
                     const int rr = r + q;
                     const uint32_t off = rr * 128 + ((((k >> 2) ^ (rr & 7))) << 4) + (k & 3) * 4;
-                    const uint32_t hi = xv[q] & 0xFFFFE000u;
+                    uint32_t hi, lo;
+                    tc::split_tf32(__uint_as_float(xv[q]), hi, lo);
                     *reinterpret_cast<uint32_t*>(ah + off) = hi;
-                    *reinterpret_cast<float*>(al + off) = __uint_as_float(xv[q]) - __uint_as_float(hi);
+                    *reinterpret_cast<uint32_t*>(al + off) = lo;
                 }
             }
             // B: already K-major; hi and lo at the same offsets
@@ -609,17 +610,13 @@ __global__ void __launch_bounds__(128, 1)
             uint4* bhp = reinterpret_cast<uint4*>(bh);
             uint4* blp = reinterpret_cast<uint4*>(bl);
 #pragma unroll 4
-            for (int i = tid; i < L::B_RAW / 16; i += 128) {
+            for (int i = tid; i < L::B_RAW / 16; i += 256) {
                 const uint4 x = rbp[i];
                 uint4 h, lo;
-                h.x = x.x & 0xFFFFE000u;
-                h.y = x.y & 0xFFFFE000u;
-                h.z = x.z & 0xFFFFE000u;
-                h.w = x.w & 0xFFFFE000u;
-                lo.x = __float_as_uint(__uint_as_float(x.x) - __uint_as_float(h.x));
-                lo.y = __float_as_uint(__uint_as_float(x.y) - __uint_as_float(h.y));
-                lo.z = __float_as_uint(__uint_as_float(x.z) - __uint_as_float(h.z));
-                lo.w = __float_as_uint(__uint_as_float(x.w) - __uint_as_float(h.w));
+                tc::split_tf32(__uint_as_float(x.x), h.x, lo.x);
+                tc::split_tf32(__uint_as_float(x.y), h.y, lo.y);
+                tc::split_tf32(__uint_as_float(x.z), h.z, lo.z);
+                tc::split_tf32(__uint_as_float(x.w), h.w, lo.w);
                 bhp[i] = h;
                 blp[i] = lo;
             }
@@ -653,31 +650,34 @@ __global__ void __launch_bounds__(128, 1)
                 ++t;  // stage t was consumed
                 break;
             }
+            // warp w: TMEM lanes 32 (w % 4) .. +31, columns of half w / 4
             tc::fence_after_sync();
             const int64_t j = t / nks;
-            const int64_t m = (blockIdx.y + j * gridDim.y) * 128 + 32 * warp + lane;
+            const int64_t m = (blockIdx.y + j * gridDim.y) * 128 + 32 * (warp & 3) + lane;
+            constexpr int HALF = NB / 2;
+            const int cb = (warp >> 2) * HALF;
 #pragma unroll 1
-            for (int c32 = 0; c32 < NB; c32 += 32) {
-                // 32 columns per round: the TMEM reads and the 32 loads of C
+            for (int c16 = 0; c16 < HALF; c16 += 16) {
+                // 16 columns per round: the TMEM reads and the 16 loads of C
                 // are all in flight before the first store
-                float d[32], c[32];
+                float d[16], c[16];
 #pragma unroll
-                for (int c8 = 0; c8 < 32 && c32 + c8 < NB; c8 += 8)
-                    tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(c32 + c8),
+                for (int c8 = 0; c8 < 16; c8 += 8)
+                    tc::tmem_ld8(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(cb + c16 + c8),
                                  *reinterpret_cast<float(*)[8]>(d + c8));
                 if (m < M) {
 #pragma unroll
-                    for (int e = 0; e < 32; ++e) {
-                        const int nn = n0 + c32 + e;
-                        c[e] = (c32 + e < NB && nn < N) ? C[m + (int64_t)nn * ldc] : 0.f;
+                    for (int e = 0; e < 16; ++e) {
+                        const int nn = n0 + cb + c16 + e;
+                        c[e] = (nn < N) ? C[m + (int64_t)nn * ldc] : 0.f;
                     }
                 }
                 tc::tmem_ld_wait();
                 if (m < M) {
 #pragma unroll
-                    for (int e = 0; e < 32; ++e) {
-                        const int nn = n0 + c32 + e;
-                        if (c32 + e < NB && nn < N) C[m + (int64_t)nn * ldc] = c[e] + alpha * d[e];
+                    for (int e = 0; e < 16; ++e) {
+                        const int nn = n0 + cb + c16 + e;
+                        if (nn < N) C[m + (int64_t)nn * ldc] = c[e] + alpha * d[e];
                     }
                 }
             }
@@ -716,7 +716,7 @@ bool launch_nn_tma(int64_t M, int N, int K, float alpha, const float* A, int64_t
     const int ntn = (N + NB - 1) / NB;
     const int64_t nblk = (M + 127) / 128;
     const int gy = (int)std::max<int64_t>(1, std::min<int64_t>(nblk, (device_sm_count() + ntn - 1) / ntn));
-    tc_nn_tma_kernel<NB><<<dim3((unsigned)ntn, (unsigned)gy), 128, NnTma<NB>::SMEM, s>>>(
+    tc_nn_tma_kernel<NB><<<dim3((unsigned)ntn, (unsigned)gy), 256, NnTma<NB>::SMEM, s>>>(
         M, N, K, alpha, C, ldc, ta, tb, err, wait_tries().load(std::memory_order_relaxed));
     return true;
 }
