@@ -97,6 +97,18 @@ __device__ __forceinline__ void warp_reduce_to_smem_x(float (&p)[NV], float* row
 __device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double recip(double x) { return 1.0 / x; }
 
+// Programmatic dependent launch.  A kernel of a call's chain is launched
+// with launch_pdl (internal.h), so it may be scheduled while the previous
+// kernel of its stream is still running.  It calls pdl_begin() first: that
+// lets the kernel after it be scheduled too (once every CTA of this grid has
+// got this far), then waits until the previous grid has completed and its
+// memory is visible.  Nothing before it touches global memory.  Launched
+// without the attribute, both instructions do nothing.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 __host__ __device__ inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
 

@@ -7,6 +7,7 @@
 
 #include <atomic>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 #include "../../include/tsqr_gb300.h"
@@ -46,6 +47,28 @@ class PerDeviceOnce {
     std::atomic<uint64_t> done_{0};
     std::mutex mu_;
 };
+
+// Launches kernel<<<grid, block, smem, s>>>(args...) with programmatic
+// stream serialization: the kernel may be scheduled before the previous
+// kernel of the stream has finished, and waits for it in pdl_begin()
+// (common.cuh), which every kernel launched this way calls first.  This
+// hides the launch and prologue of each kernel of a call's chain behind the
+// tail of the one before.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // TMA tensor map of a column-major FP32 matrix (rows x cols, leading
 // dimension ld) for boxes of box_rows x box_cols; rows and columns past the

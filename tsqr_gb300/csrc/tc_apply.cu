@@ -64,6 +64,7 @@ constexpr int tc_apply_threads() {
 template <int NMAX, int B, bool NF>
 __global__ void __launch_bounds__(tc_apply_threads<NMAX>(), NMAX <= 32 ? 4 : 1)
     tc_apply_tiles(ApplyParams<float> p, int* err, int tries) {
+    pdl_begin();
     static_assert(NMAX % 16 == 0 && NMAX <= 64 && B % 128 == 0, "bad shape");
     constexpr int NT = tc_apply_threads<NMAX>();
     constexpr int HC = NMAX * 128 / NT;  // columns a thread owns in the block phase
@@ -290,9 +291,9 @@ void launch(const ApplyParams<float>& p, int grid, int* err, cudaStream_t s) {
     const int tries = wait_tries().load(std::memory_order_relaxed);
     constexpr int NT = tc_apply_threads<NMAX>();
     if (p.n == NMAX)
-        tc_apply_tiles<NMAX, B, true><<<grid, NT, smem, s>>>(p, err, tries);
+        launch_pdl(tc_apply_tiles<NMAX, B, true>, dim3(grid), dim3(NT), smem, s, p, err, tries);
     else
-        tc_apply_tiles<NMAX, B, false><<<grid, NT, smem, s>>>(p, err, tries);
+        launch_pdl(tc_apply_tiles<NMAX, B, false>, dim3(grid), dim3(NT), smem, s, p, err, tries);
 }
 
 }  // namespace

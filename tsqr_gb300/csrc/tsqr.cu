@@ -71,7 +71,7 @@ struct TileCfg {
     static constexpr int ARPT = NT * RPT / ANT;
     static constexpr int kRows = NT * RPT;
     static void factor(const FactorParams<T>& p, int grid, cudaStream_t s) {
-        factor_tiles<T, NMAX, NT, RPT, MINB, NORM64><<<grid, NT, 0, s>>>(p);
+        launch_pdl(factor_tiles<T, NMAX, NT, RPT, MINB, NORM64>, dim3(grid), dim3(NT), 0, s, p);
     }
     static void apply(const ApplyParams<T>& p, int grid, cudaStream_t s) {
         constexpr size_t smem = apply_smem_bytes<T, NMAX, ANT * ARPT>();
@@ -80,7 +80,7 @@ struct TileCfg {
             cudaFuncSetAttribute(apply_tiles<T, NMAX, ANT, ARPT, AMINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
         });
-        apply_tiles<T, NMAX, ANT, ARPT, AMINB><<<grid, ANT, smem, s>>>(p);
+        launch_pdl(apply_tiles<T, NMAX, ANT, ARPT, AMINB>, dim3(grid), dim3(ANT), smem, s, p);
     }
 };
 
@@ -98,11 +98,14 @@ struct SplitCfg {
         // kernel would spend 7/8 of them on zero rows.
         constexpr int W32 = 32 * (NMAX / CW);
         if constexpr (RPT > 2 && NMAX <= 64)
-            if (p.ntiles == 1 && p.h <= 64) return factor_split_tiles<T, NMAX, CW, 2, 1, N64><<<1, W32, 0, s>>>(p);
+            if (p.ntiles == 1 && p.h <= 64)
+                return (void)launch_pdl(factor_split_tiles<T, NMAX, CW, 2, 1, N64>, dim3(1), dim3(W32), 0, s, p);
         if constexpr (RPT > 4)
-            if (p.ntiles == 1 && p.h <= 128) return factor_split_tiles<T, NMAX, CW, 4, 1, N64><<<1, W32, 0, s>>>(p);
+            if (p.ntiles == 1 && p.h <= 128)
+                return (void)launch_pdl(factor_split_tiles<T, NMAX, CW, 4, 1, N64>, dim3(1), dim3(W32), 0, s, p);
         if constexpr (RPT > 8)
-            if (p.ntiles == 1 && p.h <= 256) return factor_split_tiles<T, NMAX, CW, 8, 1, N64><<<1, W32, 0, s>>>(p);
+            if (p.ntiles == 1 && p.h <= 256)
+                return (void)launch_pdl(factor_split_tiles<T, NMAX, CW, 8, 1, N64>, dim3(1), dim3(W32), 0, s, p);
         if constexpr (std::is_same<T, float>::value && RPT == 16 && NMAX <= 32 && !N64) {
             // levels with several tiles per resident CTA: tiles staged by TMA
             // into shared memory, the next one copied while the current one
@@ -121,10 +124,11 @@ struct SplitCfg {
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
                 });
                 const int g = (int)std::min<int64_t>(p.ntiles, resident);
-                return factor_split_tiles_tma<T, NMAX, CW, RPT, MINB><<<g, W32, smem, s>>>(p, map);
+                return (void)launch_pdl(factor_split_tiles_tma<T, NMAX, CW, RPT, MINB>, dim3(g), dim3(W32), smem, s,
+                                        p, map);
             }
         }
-        factor_split_tiles<T, NMAX, CW, RPT, MINB, N64><<<grid, W32, 0, s>>>(p);
+        launch_pdl(factor_split_tiles<T, NMAX, CW, RPT, MINB, N64>, dim3(grid), dim3(W32), 0, s, p);
     }
     static void apply(const ApplyParams<T>& p, int grid, cudaStream_t s) {
         TileCfg<T, NMAX, ANT, ARPT, 1, AMINB>::apply(p, grid, s);

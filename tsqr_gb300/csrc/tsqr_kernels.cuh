@@ -328,6 +328,7 @@ __device__ __forceinline__ void factor_tile(FactorSmem<T, NMAX, NT, NORM64>& S, 
 
 template <typename T, int NMAX, int NT, int RPT, int MINB, bool NORM64>
 __global__ void __launch_bounds__(NT, MINB) factor_tiles(FactorParams<T> p) {
+    pdl_begin();
     constexpr int B = NT * RPT;
     __shared__ FactorSmem<T, NMAX, NT, NORM64> S;
     for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
@@ -755,6 +756,7 @@ __device__ __forceinline__ void factor_split_tile(SplitFactorSmem<T, NMAX, CW, R
 
 template <typename T, int NMAX, int CW, int RPT, int MINB, bool N64 = false>
 __global__ void __launch_bounds__(32 * (NMAX / CW), MINB) factor_split_tiles(FactorParams<T> p) {
+    pdl_begin();
     constexpr int B = 32 * RPT;
     __shared__ SplitFactorSmem<T, NMAX, CW, RPT> S;
     for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
@@ -810,6 +812,7 @@ struct TmaNextTile {
 template <typename T, int NMAX, int CW, int RPT, int MINB>
 __global__ void __launch_bounds__(32 * (NMAX / CW), MINB)
     factor_split_tiles_tma(FactorParams<T> p, const __grid_constant__ CUtensorMap tmap) {
+    pdl_begin();
     static_assert(RPT % 8 == 0, "tiles of whole 256-row boxes");
     constexpr int B = 32 * RPT, BOXES = RPT / 8, BOX_BYTES = NMAX * 256 * (int)sizeof(T);
     __shared__ SplitFactorSmem<T, NMAX, CW, RPT> S;
@@ -1051,6 +1054,7 @@ __device__ __forceinline__ void apply_tile(unsigned char* apply_smem, T* tile, i
 
 template <typename T, int NMAX, int NT, int RPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) apply_tiles(ApplyParams<T> p) {
+    pdl_begin();
     constexpr int B = NT * RPT;
     extern __shared__ __align__(16) unsigned char apply_smem[];
     for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
