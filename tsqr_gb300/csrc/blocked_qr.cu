@@ -38,6 +38,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) gemm_tn_partial(int M, int N, int64_t K, const T* __restrict__ A,
                                                        int64_t lda, const T* __restrict__ B, int64_t ldb,
                                                        T* __restrict__ P, int64_t kchunk) {
+    pdl_begin();
     __shared__ T As[kKt][kTile + 1];
     __shared__ T Bs[kKt][kTile + 1];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -102,6 +103,7 @@ __global__ void __launch_bounds__(256) gemm_tn_partial(int M, int N, int64_t K, 
 template <typename T>
 __global__ void __launch_bounds__(256) reduce_partials(int M, int N, int nz, const T* __restrict__ P, T alpha,
                                                        T beta, T* C, int64_t ldc) {
+    pdl_begin();
     __shared__ T s[8][32];
     const int64_t total = (int64_t)M * N;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -278,6 +280,7 @@ constexpr size_t kPTmaSmem = kPStages * kPStageBytes + 1024;  // + alignment of 
 
 __global__ void __launch_bounds__(256, 3)
     gemm_tn_tma(TnFusedArgs p, const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb) {
+    pdl_begin();
     extern __shared__ unsigned char tn_raw[];
     __shared__ unsigned long long mbar[kPStages];
     __shared__ int s_last;
@@ -370,6 +373,7 @@ __global__ void __launch_bounds__(256, 3)
 
 template <bool VEC>
 __global__ void __launch_bounds__(256, 3) gemm_tn_fused(TnFusedArgs p) {
+    pdl_begin();
     __shared__ __align__(16) float sm[2 * kPRows * kPT];  // A step | B step; later the four K slices' tiles
     __shared__ int s_last;
     float* As = sm;
@@ -494,6 +498,7 @@ size_t nn_fused_smem(int n1) { return ((size_t)round_up(n1, kNK) * kNXs + (size_
 
 template <bool VEC>
 __global__ void __launch_bounds__(256, 2) gemm_nn_fused(NnFusedArgs p) {
+    pdl_begin();
     extern __shared__ __align__(16) float nn_smem[];
     const int n1p = (p.n1 + kNK - 1) / kNK * kNK;
     float* Xs = nn_smem;              // [n1p][kNXs]
@@ -612,6 +617,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) gemm_nn(int64_t M, int N, int K, T alpha, const T* __restrict__ A,
                                                int64_t lda, const T* __restrict__ B, int64_t ldb, T beta, T* C,
                                                int64_t ldc) {
+    pdl_begin();
     __shared__ T As[kKt][kTile + 1];
     __shared__ T Bs[kKt][kTile + 1];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -677,6 +683,7 @@ __global__ void __launch_bounds__(256) gemm_nn(int64_t M, int N, int K, T alpha,
 
 template <typename T>
 __global__ void axpy_block(int M, int N, const T* __restrict__ X, int64_t ldx, T* Y, int64_t ldy) {
+    pdl_begin();
     const int64_t total = (int64_t)M * N;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -761,7 +768,8 @@ void proj_tn_tc(int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2, int
     if constexpr (std::is_same<T, float>::value) {
         const int nz = tc_gemm_tn((int)n1, (int)n2, m, A1, lda, A2, lda, P, err, s, bf16);
         log_launch(kTagTc + 100, s);
-        reduce_partials<T><<<reduce_blocks(n1 * n2), 256, 0, s>>>((int)n1, (int)n2, nz, P, T(1), beta, C, ldc);
+        launch_pdl(reduce_partials<T>, dim3(reduce_blocks(n1 * n2)), dim3(256), 0, s, (int)n1, (int)n2, nz,
+                   (const T*)P, T(1), beta, C, ldc);
         log_launch(kTagReduce, s);
     }
 }
@@ -793,9 +801,9 @@ void update_nn_fused(int64_t m, int64_t n1, int64_t n2, const float* A1, int64_t
     const bool vec = lda % 4 == 0 && reinterpret_cast<uintptr_t>(A1) % 16 == 0 &&
                      reinterpret_cast<uintptr_t>(A2) % 16 == 0;
     if (vec)
-        gemm_nn_fused<true><<<dim3((unsigned)gx, (unsigned)tj), 256, smem, s>>>(a);
+        launch_pdl(gemm_nn_fused<true>, dim3((unsigned)gx, (unsigned)tj), dim3(256), smem, s, a);
     else
-        gemm_nn_fused<false><<<dim3((unsigned)gx, (unsigned)tj), 256, smem, s>>>(a);
+        launch_pdl(gemm_nn_fused<false>, dim3((unsigned)gx, (unsigned)tj), dim3(256), smem, s, a);
     log_launch(kTagGemmNN, s);
 }
 
@@ -824,7 +832,7 @@ void update_nn(int64_t m, int64_t n1, int64_t n2, const T* A1, int64_t lda, cons
         if (n1 <= kNMaxK) return update_nn_fused(m, n1, n2, A1, lda, X, ldx, A2, s);
     }
     dim3 g((unsigned)ceil_div(m, kTile), (unsigned)ceil_div(n2, kTile));
-    gemm_nn<T><<<g, 256, 0, s>>>(m, (int)n2, (int)n1, T(-1), A1, lda, X, ldx, T(1), A2, lda);
+    launch_pdl(gemm_nn<T>, g, dim3(256), 0, s, m, (int)n2, (int)n1, T(-1), A1, lda, X, ldx, T(1), A2, lda);
     log_launch(kTagGemmNN, s);
 }
 
@@ -865,24 +873,25 @@ tsqr_status proj_tn(int64_t m, int64_t n1, int64_t n2, const T* A1, const T* A2,
             attr.run([] {
                 cudaFuncSetAttribute(gemm_tn_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPTmaSmem);
             });
-            gemm_tn_tma<<<g, 256, kPTmaSmem, s>>>(a, ta, tb);
+            launch_pdl(gemm_tn_tma, g, dim3(256), kPTmaSmem, s, a, ta, tb);
             log_launch(kTagGemmTN, s);
             return TSQR_OK;
         }
         const bool vec = lda % 4 == 0 && reinterpret_cast<uintptr_t>(A1) % 16 == 0 &&
                          reinterpret_cast<uintptr_t>(A2) % 16 == 0;
         if (vec)
-            gemm_tn_fused<true><<<g, 256, 0, s>>>(a);
+            launch_pdl(gemm_tn_fused<true>, g, dim3(256), 0, s, a);
         else
-            gemm_tn_fused<false><<<g, 256, 0, s>>>(a);
+            launch_pdl(gemm_tn_fused<false>, g, dim3(256), 0, s, a);
         log_launch(kTagGemmTN, s);
         return TSQR_OK;
     }
     GemmPlan gp = tn_plan(n1, n2, m);
     dim3 g((unsigned)ceil_div(n1, kTile), (unsigned)ceil_div(n2, kTile), (unsigned)gp.nz);
-    gemm_tn_partial<T><<<g, 256, 0, s>>>((int)n1, (int)n2, m, A1, lda, A2, lda, P, gp.kchunk);
+    launch_pdl(gemm_tn_partial<T>, g, dim3(256), 0, s, (int)n1, (int)n2, m, A1, lda, A2, lda, P, gp.kchunk);
     log_launch(kTagGemmTN, s);
-    reduce_partials<T><<<reduce_blocks(n1 * n2), 256, 0, s>>>((int)n1, (int)n2, gp.nz, P, T(1), beta, C, ldc);
+    launch_pdl(reduce_partials<T>, dim3(reduce_blocks(n1 * n2)), dim3(256), 0, s, (int)n1, (int)n2, gp.nz,
+               (const T*)P, T(1), beta, C, ldc);
     log_launch(kTagReduce, s);
     return TSQR_OK;
 }
@@ -935,7 +944,8 @@ tsqr_status qr_rec(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, c
             update_nn<T>(m, n1, n2, A1, lda, tmp, n1, A2, s);
         }
         int blocks = (int)std::min<int64_t>(ceil_div(n1 * n2, 256), 1024);
-        axpy_block<T><<<blocks, 256, 0, s>>>((int)n1, (int)n2, tmp, n1, R12, ldr);
+        launch_pdl(axpy_block<T>, dim3(blocks), dim3(256), 0, s, (int)n1, (int)n2, (const T*)tmp, (int64_t)n1, R12,
+                   ldr);
         log_launch(kTagAxpy, s);
     }
     if (cudaMemset2DAsync(R + n1, ldr * sizeof(T), 0, n2 * sizeof(T), n1, s) != cudaSuccess) return TSQR_ERR_CUDA;
@@ -967,6 +977,7 @@ constexpr int kHrMax = 32;  // panel width limit of the Householder path
 template <typename T>
 __global__ void __launch_bounds__(256) hr_reconstruct(int bw, T* Ap, int64_t lda, const T* Rp, int ldrp, T* Uinv,
                                                       T* Tp, int64_t ldt, T* Rout, int64_t ldr) {
+    pdl_begin();
     __shared__ T W[kHrMax][kHrMax + 1];   // LU in place: U on and above, L below the diagonal
     __shared__ T Ui[kHrMax][kHrMax + 1];  // U^-1
     __shared__ T Li[kHrMax][kHrMax + 1];  // Y_1^-1 (unit lower)
@@ -1024,6 +1035,7 @@ __global__ void __launch_bounds__(256) hr_reconstruct(int bw, T* Ap, int64_t lda
 // triangular), in place, one thread per row.
 template <typename T>
 __global__ void __launch_bounds__(256) rows_times_uinv(int64_t rows, int bw, T* Y, int64_t lda, const T* Uinv) {
+    pdl_begin();
     __shared__ T U[kHrMax][kHrMax];
     for (int e = threadIdx.x; e < kHrMax * kHrMax; e += blockDim.x) {
         const int i = e % kHrMax, j = e / kHrMax;
@@ -1052,6 +1064,7 @@ __global__ void __launch_bounds__(256) rows_times_uinv(int64_t rows, int bw, T* 
 template <typename T>
 __global__ void tri_mul(int kind, int p, int64_t q, const T* U, int64_t ldu, const T* W, int64_t ldw, T alpha, T* X,
                         int64_t ldx) {
+    pdl_begin();
     const int64_t total = (int64_t)p * q;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(e % p);
@@ -1072,6 +1085,7 @@ __global__ void tri_mul(int kind, int p, int64_t q, const T* U, int64_t ldu, con
 // T(i,k) Y_1(c,k).
 template <typename T>
 __global__ void panel_m(int bw, const T* Y, int64_t lda, const T* Tp, int64_t ldt, T* M) {
+    pdl_begin();
     for (int e = threadIdx.x; e < bw * bw; e += blockDim.x) {
         const int i = e % bw, c = e / bw;
         T x = T(0);
@@ -1084,6 +1098,7 @@ __global__ void panel_m(int bw, const T* Y, int64_t lda, const T* Tp, int64_t ld
 // thread per row (each row reads only itself).
 template <typename T>
 __global__ void __launch_bounds__(256) panel_q_rows(int64_t rows, int bw, T* Y, int64_t lda, const T* M) {
+    pdl_begin();
     __shared__ T Ms[kHrMax][kHrMax + 1];
     for (int e = threadIdx.x; e < kHrMax * kHrMax; e += blockDim.x) {
         const int i = e % kHrMax, j = e / kHrMax;

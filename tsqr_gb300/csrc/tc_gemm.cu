@@ -24,6 +24,7 @@
 
 #include <algorithm>
 
+#include "common.cuh"
 #include "internal.h"
 #include "tc.cuh"
 
@@ -51,6 +52,7 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int64_t K, c
                                                       const float* __restrict__ Bm, int64_t ldb, float* __restrict__ C,
                                                       int64_t ldc,
                                                       float alpha, int64_t kchunk, int* err, int tries) {
+    pdl_begin();
     extern __shared__ __align__(1024) unsigned char gemm_smem_raw[];
     GemmSmem<NB>& S = *reinterpret_cast<GemmSmem<NB>*>(gemm_smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -305,8 +307,8 @@ void launch_gemm(dim3 grid, int M, int N, int64_t K, const float* A, int64_t lda
         cudaFuncSetAttribute(tc_gemm_kernel<TRANS_A, NB, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
     });
-    tc_gemm_kernel<TRANS_A, NB, BF><<<grid, 128, smem, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, kchunk, err,
-                                                             wait_tries().load(std::memory_order_relaxed));
+    launch_pdl(tc_gemm_kernel<TRANS_A, NB, BF>, grid, dim3(128), smem, s, M, N, K, A, lda, B, ldb, C, ldc, alpha,
+               kchunk, err, wait_tries().load(std::memory_order_relaxed));
 }
 
 template <bool TRANS_A, bool BF>
@@ -348,6 +350,7 @@ __global__ void __launch_bounds__(128, 1)
     tc_tn_tma_kernel(int M, int N, int64_t K, int64_t kchunk, float* __restrict__ P,
                      const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int* err,
                      int tries) {
+    pdl_begin();
     using L = TnTma<NB>;
     extern __shared__ unsigned char tn_smem[];
     __shared__ unsigned long long full[2], mmad[2];
@@ -525,6 +528,7 @@ __global__ void __launch_bounds__(256, 1)
     tc_nn_tma_kernel(int64_t M, int N, int K, float alpha, float* __restrict__ C, int64_t ldc,
                      const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int* err,
                      int tries) {
+    pdl_begin();
     using L = NnTma<NB>;
     extern __shared__ unsigned char nn_smem[];
     __shared__ unsigned long long full[L::NRAW], mmad[2];
@@ -716,8 +720,8 @@ bool launch_nn_tma(int64_t M, int N, int K, float alpha, const float* A, int64_t
     const int ntn = (N + NB - 1) / NB;
     const int64_t nblk = (M + 127) / 128;
     const int gy = (int)std::max<int64_t>(1, std::min<int64_t>(nblk, (device_sm_count() + ntn - 1) / ntn));
-    tc_nn_tma_kernel<NB><<<dim3((unsigned)ntn, (unsigned)gy), 256, NnTma<NB>::SMEM, s>>>(
-        M, N, K, alpha, C, ldc, ta, tb, err, wait_tries().load(std::memory_order_relaxed));
+    launch_pdl(tc_nn_tma_kernel<NB>, dim3((unsigned)ntn, (unsigned)gy), dim3(256), NnTma<NB>::SMEM, s, M, N, K,
+               alpha, C, ldc, ta, tb, err, wait_tries().load(std::memory_order_relaxed));
     return true;
 }
 
@@ -733,8 +737,8 @@ bool launch_tn_tma(dim3 g, int M, int N, int64_t K, int64_t kchunk, const float*
         cudaFuncSetAttribute(tc_tn_tma_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)TnTma<NB>::SMEM);
     });
-    tc_tn_tma_kernel<NB><<<g, 128, TnTma<NB>::SMEM, s>>>(M, N, K, kchunk, P, ta, tb, err,
-                                                         wait_tries().load(std::memory_order_relaxed));
+    launch_pdl(tc_tn_tma_kernel<NB>, g, dim3(128), TnTma<NB>::SMEM, s, M, N, K, kchunk, P, ta, tb, err,
+               wait_tries().load(std::memory_order_relaxed));
     return true;
 }
 
