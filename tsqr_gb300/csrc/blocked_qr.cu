@@ -809,9 +809,11 @@ void update_nn_fused(int64_t m, int64_t n1, int64_t n2, const float* A1, int64_t
 
 // The tensor-core forms' updates run on the tcgen05 GEMM only when the
 // panel is wider than kNnTcMin.  Measured at 131,072 x 512 (TF32x3,
-// reorthogonalised): 6.156 ms with the CUDA-core kernel up to 64 columns,
-// 5.966 ms up to 128, 6.077 ms up to 256.
-constexpr int64_t kNnTcMin = 128;
+// reorthogonalised) with the register-staged tcgen05 kernel: 6.156 ms with
+// the CUDA-core kernel up to 64 columns, 5.966 ms up to 128, 6.077 ms up
+// to 256; with the TMA-fed one (tc_nn_tma_kernel, 256 threads): 4.531 ms
+// up to 128, 4.386 ms up to 64.
+constexpr int64_t kNnTcMin = 64;
 
 // A2 (m x n2) -= A1 (m x n1) X (n1 x n2) in a tensor-core form (FP32 only).
 template <typename T>

@@ -346,7 +346,7 @@ struct TnTma {
 };
 
 template <int NB>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(256, 1)
     tc_tn_tma_kernel(int M, int N, int64_t K, int64_t kchunk, float* __restrict__ P,
                      const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int* err,
                      int tries) {
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(128, 1)
             const uint4* src = reinterpret_cast<const uint4*>(base + b * L::STAGE);
             uint4* dst = reinterpret_cast<uint4*>(base + b * L::STAGE + L::RAW);
 #pragma unroll 4
-            for (int i = tid; i < L::RAW / 16; i += 128) {
+            for (int i = tid; i < L::RAW / 16; i += 256) {
                 const uint4 x = src[i];
                 uint4 lo;
                 lo.x = __float_as_uint(__uint_as_float(x.x) - __uint_as_float(x.x & 0xFFFFE000u));
@@ -469,18 +469,21 @@ __global__ void __launch_bounds__(128, 1)
                 (void)tc::mbar_wait(tc::smem_u32(&mmad[q & 1]), (uint32_t)(q >> 1) & 1u);
         }
     } else {
+        // warp w: TMEM lanes 32 (w % 4) .. +31, columns of half w / 4
         tc::fence_after_sync();
-        const int m = m0 + 32 * warp + (tid & 31);
+        const int m = m0 + 32 * (warp & 3) + (tid & 31);
         float* Pz = P + (int64_t)blockIdx.z * M * N;
+        constexpr int HALF = NB / 2;
+        const int cb = (warp >> 2) * HALF;
 #pragma unroll 2
-        for (int c8 = 0; c8 < NB; c8 += 8) {
+        for (int c8 = 0; c8 < HALF; c8 += 8) {
             float d[8];
-            tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c8, d);
+            tc::tmem_ld8(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(cb + c8), d);
             tc::tmem_ld_wait();
             if (m < M) {
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
-                    const int nn = n0 + c8 + e;
+                    const int nn = n0 + cb + c8 + e;
                     if (nn < N) Pz[m + (int64_t)nn * M] = nst > 0 ? d[e] : 0.f;
                 }
             }
@@ -737,7 +740,7 @@ bool launch_tn_tma(dim3 g, int M, int N, int64_t K, int64_t kchunk, const float*
         cudaFuncSetAttribute(tc_tn_tma_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)TnTma<NB>::SMEM);
     });
-    launch_pdl(tc_tn_tma_kernel<NB>, g, dim3(128), TnTma<NB>::SMEM, s, M, N, K, kchunk, P, ta, tb, err,
+    launch_pdl(tc_tn_tma_kernel<NB>, g, dim3(256), TnTma<NB>::SMEM, s, M, N, K, kchunk, P, ta, tb, err,
                wait_tries().load(std::memory_order_relaxed));
     return true;
 }
