@@ -78,6 +78,7 @@ __device__ __forceinline__ int find_item(const Item* it, int count, int64_t t) {
 
 template <int NMAX, int NT, int RPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batched_factor(const __grid_constant__ FactorTable tab) {
+    pdl_begin();
     constexpr int B = NT * RPT;
     __shared__ FactorSmem<float, NMAX, NT, false> S;
     for (int64_t t = blockIdx.x; t < tab.total; t += gridDim.x) {
@@ -92,6 +93,7 @@ __global__ void __launch_bounds__(NT, MINB) batched_factor(const __grid_constant
 
 template <int NMAX, int CW, int RPT, int MINB>
 __global__ void __launch_bounds__(32 * (NMAX / CW), MINB) batched_factor_split(const __grid_constant__ FactorTable tab) {
+    pdl_begin();
     constexpr int B = 32 * RPT;
     __shared__ SplitFactorSmem<float, NMAX, CW, RPT> S;
     for (int64_t t = blockIdx.x; t < tab.total; t += gridDim.x) {
@@ -106,6 +108,7 @@ __global__ void __launch_bounds__(32 * (NMAX / CW), MINB) batched_factor_split(c
 
 template <int NMAX, int NT, int RPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batched_apply(const __grid_constant__ ApplyTable tab) {
+    pdl_begin();
     constexpr int B = NT * RPT;
     extern __shared__ __align__(16) unsigned char apply_smem[];
     for (int64_t t = blockIdx.x; t < tab.total; t += gridDim.x) {
@@ -138,14 +141,14 @@ void class_apply(const ApplyTable& t, int grid, cudaStream_t s) {
         cudaFuncSetAttribute(batched_apply<NMAX, ANT, ARPT, AMINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kSmem);
     });
-    batched_apply<NMAX, ANT, ARPT, AMINB><<<grid, ANT, kSmem, s>>>(t);
+    launch_pdl(batched_apply<NMAX, ANT, ARPT, AMINB>, dim3(grid), dim3(ANT), kSmem, s, t);
 }
 
 // one thread per row slice (factor_tile)
 template <int NMAX, int NT, int RPT, int MINB, int AMINB, int ANT = NT>
 struct Cls {
     static void factor(const FactorTable& t, int grid, cudaStream_t s) {
-        batched_factor<NMAX, NT, RPT, MINB><<<grid, NT, 0, s>>>(t);
+        launch_pdl(batched_factor<NMAX, NT, RPT, MINB>, dim3(grid), dim3(NT), 0, s, t);
     }
     static ClassCfg cfg() { return {NMAX, NT * RPT, MINB, AMINB, &factor, &class_apply<NMAX, NT * RPT, ANT, AMINB>}; }
 };
@@ -154,7 +157,7 @@ struct Cls {
 template <int NMAX, int CW, int RPT, int MINB, int AMINB, int ANT>
 struct SplitCls {
     static void factor(const FactorTable& t, int grid, cudaStream_t s) {
-        batched_factor_split<NMAX, CW, RPT, MINB><<<grid, 32 * (NMAX / CW), 0, s>>>(t);
+        launch_pdl(batched_factor_split<NMAX, CW, RPT, MINB>, dim3(grid), dim3(32 * (NMAX / CW)), 0, s, t);
     }
     static ClassCfg cfg() { return {NMAX, 32 * RPT, MINB, AMINB, &factor, &class_apply<NMAX, 32 * RPT, ANT, AMINB>}; }
 };

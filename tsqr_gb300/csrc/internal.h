@@ -54,6 +54,21 @@ class PerDeviceOnce {
 // (common.cuh), which every kernel launched this way calls first.  This
 // hides the launch and prologue of each kernel of a call's chain behind the
 // tail of the one before.
+// A call whose kernels wait on copies of another stream (the host-buffer
+// entry points) turns the attribute off for its launches with a PdlOff
+// scope: with it, kernels scheduled early waited in pdl_begin() on SMs that
+// the copies' completion then had to share, and tsqr_s_host at 4,194,304 x
+// 32 took 43.5 ms instead of 5.7 ms.
+inline bool& pdl_allowed() {
+    thread_local bool v = true;
+    return v;
+}
+struct PdlOff {
+    bool prev;
+    PdlOff() : prev(pdl_allowed()) { pdl_allowed() = false; }
+    ~PdlOff() { pdl_allowed() = prev; }
+};
+
 template <typename... KArgs, typename... Args>
 cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
                        Args&&... args) {
@@ -64,7 +79,7 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    attr[0].val.programmaticStreamSerializationAllowed = pdl_allowed() ? 1 : 0;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);

@@ -514,6 +514,7 @@ size_t tsqr_host_workspace(int64_t m, int64_t n, bool prec) {
 template <typename T>
 tsqr_status tsqr_host(int64_t m, int64_t n, const T* hA, int64_t lda, T* hQ, int64_t ldq, T* hR, int64_t ldr,
                       void* work, size_t work_bytes, bool prec, cudaStream_t s) {
+    const PdlOff no_pdl;  // the kernels below wait on the copy stream's events
     const HostLayout<T> HL = host_layout<T>(m, n, prec);
     if (HL.total == 0) return TSQR_ERR_UNSUPPORTED;
     if (work == nullptr || work_bytes < HL.total) return TSQR_ERR_WORKSPACE;
