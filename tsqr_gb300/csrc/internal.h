@@ -58,14 +58,19 @@ class PerDeviceOnce {
 // entry points) turns the attribute off for its launches with a PdlOff
 // scope: with it, kernels scheduled early waited in pdl_begin() on SMs that
 // the copies' completion then had to share, and tsqr_s_host at 4,194,304 x
-// 32 took 43.5 ms instead of 5.7 ms.
+// 32 took 43.5 ms instead of 5.7 ms.  TSQR wider than 32 columns turns it
+// off too: its kernels fill an SM with one CTA, so nothing overlaps, and
+// the call at 4,194,304 x 64 was 0.7% slower with it (5.157 against
+// 5.122 ms).
 inline bool& pdl_allowed() {
     thread_local bool v = true;
     return v;
 }
 struct PdlOff {
     bool prev;
-    PdlOff() : prev(pdl_allowed()) { pdl_allowed() = false; }
+    explicit PdlOff(bool off = true) : prev(pdl_allowed()) {
+        if (off) pdl_allowed() = false;
+    }
     ~PdlOff() { pdl_allowed() = prev; }
 };
 

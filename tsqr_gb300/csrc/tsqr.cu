@@ -217,6 +217,7 @@ size_t tsqr_plain_workspace(int64_t m, int64_t n) {
 template <typename T>
 tsqr_status tsqr_plain(int64_t m, int64_t n, T* A, int64_t lda, T* R, int64_t ldr, void* work, size_t work_bytes,
                        cudaStream_t s, int phases) {
+    const PdlOff no_pdl(n > 32);
     KernelSet<T> ks = pick((T*)nullptr, (int)n);
     if (!ks.factor) return TSQR_ERR_UNSUPPORTED;
     std::vector<Level<T>> lv;
@@ -354,6 +355,7 @@ size_t tsqr_precision_workspace(int64_t m, int64_t n, PrecFlags f) {
 
 tsqr_status tsqr_precision(int64_t m, int64_t n, float* A, int64_t lda, float* R, int64_t ldr, void* work,
                            size_t work_bytes, cudaStream_t s, PrecFlags f) {
+    const PdlOff no_pdl(n > 32);
     PrecCfg c = pick_precision((int)n, f.norm64);
     if (!c.ks.factor) return TSQR_ERR_UNSUPPORTED;
     if (f.root64 && n > 32) return TSQR_ERR_UNSUPPORTED;
