@@ -101,6 +101,12 @@ def test_no_new_or_larger_spills(spills):
 @pytest.mark.parametrize("kernel", ["tsqr::factor_split_tiles<float, 32, 4, 16, 2, false>",
                                     "tsqr::factor_split_tiles<float, 16, 4, 16, 4, false>",
                                     "tsqr::apply_tiles<float, 32, 256, 2, 2>",
-                                    "tsqr::tc_apply_tiles<32, 512, true>"])
+                                    "tsqr::tc_apply_tiles<32, 512, true>",
+                                    "tsqr::tc_apply_tiles<64, 512, true>",
+                                    "tsqr::gemm_tn_tma",
+                                    "tsqr::gemm_nn_fused<true>",
+                                    "tsqr::tc_tn_tma_kernel<256>",
+                                    "tsqr::tc_nn_tma_kernel<128>"])
 def test_headline_kernels_do_not_spill(spills, kernel):
     assert kernel not in spills
+
