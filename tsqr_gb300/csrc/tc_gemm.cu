@@ -330,12 +330,14 @@ int nb_for(int N) { return N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256)
 // K arrives as boxes of 32 x 128 (A) and 32 x NB (B) with the 128-byte
 // swizzle, which is the layout the MMA reads (smem_desc_sw128).  The raw
 // FP32 tile is the hi operand (TF32 reads the top 19 bits); one pass of the
-// CTA writes lo = x - trunc(x) beside it at the same offsets, and one thread
-// issues hi*hi + hi*lo + lo*hi for the 4 K steps of 8.  Two stages: the
-// copy of stage s+2 is issued once the MMAs of stage s have read its
-// buffers.  Every wait is bounded; a CTA whose wait gives up sets the
-// status word, waits (with the full limit) for its copies and MMAs in
-// flight, frees its TMEM and stops.
+// CTA (256 threads) writes lo = x - trunc(x) beside it at the same offsets,
+// and one thread issues hi*hi + hi*lo + lo*hi for the 4 K steps of 8.  Two
+// stages: the copy of stage s+2 is issued once the MMAs of stage s have
+// read its buffers.  The epilogue splits the TMEM read-back by column
+// halves: warp w reads lanes 32 (w % 4) .. +31 of half w / 4.  Every wait
+// is bounded; a CTA whose wait gives up sets the status word, waits (with
+// the full limit) for its copies and MMAs in flight, frees its TMEM and
+// stops.
 template <int NB>
 struct TnTma {
     static constexpr int A_BYTES = 128 * 128;             // 128 rows of 32 FP32
@@ -510,10 +512,11 @@ __global__ void __launch_bounds__(256, 1)
 // copy's buffer is free once the CTA has rewritten it: the copies run in a
 // ring of three stages (the copy of step t+3 is issued right after step t's
 // rewrite), the operand tiles in two buffers (step t's rewrite waits for the
-// MMAs of step t-2).  A persistent CTA (one per SM) walks 128-row blocks; a
-// block's K stages accumulate in TMEM, and its epilogue reads C 32 columns
-// at a time, adds alpha D and writes it back.  Bounded waits as in the
-// projection kernel.
+// MMAs of step t-2).  A persistent CTA (one per SM, 256 threads: warp w
+// rewrites row groups 4w..4w+3) walks 128-row blocks; a block's K stages
+// accumulate in TMEM, and its epilogue (warp w: TMEM lanes 32 (w % 4) ..
+// +31, columns of half w / 4) reads C 16 columns at a time, adds alpha D
+// and writes it back.  Bounded waits as in the projection kernel.
 template <int NB>
 struct NnTma {
     static constexpr int A_RAW = 128 * 128;            // four 32 x 32 boxes
@@ -748,7 +751,7 @@ bool launch_tn_tma(dim3 g, int M, int N, int64_t K, int64_t kchunk, const float*
 }  // namespace
 
 int tc_tn_splits(int64_t M, int64_t N, int64_t K) {
-    // one wave of one CTA per SM on GB300's 152 SMs (the TMA form's 192 KB
+    // one wave of one CTA per SM on GB300's 152 SMs (the TMA form's 193 KB
     // of shared memory); the workspace query uses the same count
     const int64_t tiles = ((M + 127) / 128) * ((N + 255) / 256);
     int64_t nz = std::max<int64_t>(1, (152 + tiles - 1) / tiles);
