@@ -420,7 +420,9 @@ def batched_table():
 
 
 def tsqr_batched_(As, Rs=None, precision="plain", work=None, stream=None):
-    """Factor a list of column-major float32 CUDA tensors in one launch."""
+    """Factor a list of column-major float32 CUDA tensors in one call: one
+    launch per tree level and width class, no allocation and no host-to-device
+    copy, so the call can be captured into a CUDA graph and replayed."""
     import torch
     count = len(As)
     if Rs is None:
