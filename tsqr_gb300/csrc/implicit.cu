@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/tsqr_gb300.h"
+#include "common.cuh"
 #include "internal.h"
 
 namespace tsqr {
@@ -73,6 +74,7 @@ struct QtParams {
 
 template <typename T, int NMAX>
 __global__ void __launch_bounds__(kNT) apply_qt_tiles(QtParams<T, NMAX> p) {
+    pdl_begin();
     extern __shared__ __align__(16) unsigned char qt_smem_raw[];
     QtSmem<T, NMAX>& S = *reinterpret_cast<QtSmem<T, NMAX>*>(qt_smem_raw);
     constexpr int JPT = NMAX / 8;  // outputs j per thread (8 warps x JPT = NMAX)
@@ -195,6 +197,7 @@ __device__ __forceinline__ T warp_reduce_scatter32(T (&v)[32], int lane) {
 // streams the level at close to the memory rate.  Tile heights up to 1024.
 template <typename T, int NMAX>
 __global__ void __launch_bounds__(kNT) apply_qt_column(QtParams<T, NMAX> p, int64_t col) {
+    pdl_begin();
     constexpr int NW = kNT / 32;
     __shared__ T ys[NW][NMAX];
     __shared__ T yv[NMAX], zv[NMAX];
@@ -262,7 +265,7 @@ cudaError_t launch_apply_qt(const QtParams<T, NMAX>& p, cudaStream_t s) {
         // kernel at any k up to 32)
         const int sms = device_sm_count();
         const int grid = (int)std::min<int64_t>(p.ntiles, (int64_t)sms * 8);
-        for (int64_t c = 0; c < p.k; ++c) apply_qt_column<T, NMAX><<<grid, kNT, 0, s>>>(p, c);
+        for (int64_t c = 0; c < p.k; ++c) launch_pdl(apply_qt_column<T, NMAX>, dim3(grid), dim3(kNT), 0, s, p, c);
         return cudaGetLastError();
     }
     constexpr size_t smem = sizeof(QtSmem<T, NMAX>);
@@ -276,7 +279,7 @@ cudaError_t launch_apply_qt(const QtParams<T, NMAX>& p, cudaStream_t s) {
     if (attr != cudaSuccess) return attr;
     const int64_t items = p.ntiles * ((p.k + kKB - 1) / kKB);
     const int grid = (int)std::min<int64_t>(items, 1 << 20);
-    apply_qt_tiles<T, NMAX><<<grid, kNT, smem, s>>>(p);
+    launch_pdl(apply_qt_tiles<T, NMAX>, dim3(grid), dim3(kNT), smem, s, p);
     return cudaGetLastError();
 }
 
